@@ -1,0 +1,366 @@
+#!/usr/bin/env python
+"""Frame-loop benchmark of the GB300 KinectFusion path.
+
+One step = one IncomingFrameProcessing (vertex/normal map, single-level 10-iteration
+ICP, TSDF integration, ray cast) on a 640x480 depth frame into the reference's
+default 360x360x300 TSDF at 10 mm (workload c1).  Input: a seeded synthetic
+sequence (analytic room, Kinect v1 noise model), played forwards then backwards so
+the trajectory stays continuous for any step count.
+
+  value   frames/s with the depth frames already in device memory (all ranks)
+  e2e     frames/s through the C ABI with host buffers: each frame's uint16 depth is
+          copied from pinned host memory and the pose read back to the host
+  roofline, cpu_baseline, clocks, stage times: see the design doc
+
+--impl reference times the reference's own kernel bodies compiled for the host CPU
+(oracle/_ref, or the oracle restatement where that could not be built) on the same
+workload, with every host core.
+
+Multi-GPU (--gpus N under torchrun): independent replicas, one scene per GPU, no
+collective on the data path; the timed region is bracketed by barriers and the max
+over ranks is reported.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "frames/s (640x480, 360x360x300 TSDF) FP16-TSDF vs FP32 form at <=1 mm ATE"
+UNIQUE_FRAMES = 48
+
+
+def parse_args(argv=None):
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=300)
+    p.add_argument("--warmup", type=int, default=10)
+    p.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    p.add_argument("--config", default="c1")
+    p.add_argument("--tsdf", choices=["f32", "f16"], default="f32")
+    p.add_argument("--profile-frames", type=int, default=30, help="frames with per-stage CUDA events")
+    p.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample budget")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
+    return p.parse_args(argv)
+
+
+def pingpong(n_unique: int, n: int) -> list[int]:
+    """0, 1, ..., n_unique-1, n_unique-2, ..., 1, 0, 1, ... (a continuous trajectory)."""
+    period = max(1, 2 * (n_unique - 1))
+    out = []
+    for k in range(n):
+        r = k % period if n_unique > 1 else 0
+        out.append(r if r < n_unique else period - r)
+    return out
+
+
+class Dist:
+    """torch.distributed plumbing for replicas: barrier and max over ranks only."""
+
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+
+            backend = "nccl" if os.environ.get("KF_BENCH_BACKEND", "nccl") == "nccl" else "gloo"
+            dist.init_process_group(backend=backend)
+            self.pg = dist
+            self.backend = backend
+
+    def barrier(self):
+        if self.pg:
+            if self.backend == "nccl":
+                import torch
+
+                self.pg.barrier(device_ids=[self.local_rank])
+            else:
+                self.pg.barrier()
+
+    def max(self, x: float) -> float:
+        if not self.pg:
+            return x
+        import torch
+
+        dev = f"cuda:{self.local_rank}" if self.backend == "nccl" else "cpu"
+        t = torch.tensor([x], dtype=torch.float64, device=dev)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle-reason samples while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.out = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-i", str(self.device), "-lms", "200"], stdout=self.out,
+                                         stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        self.proc.wait()
+        self.out.flush()
+        self.out.seek(0)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.out.read().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        os.unlink(self.out.name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def workload(args):
+    from kinect_fusion_slam_gb300 import scene
+
+    cfg = scene.config(args.config)
+    return cfg
+
+
+def config_desc(cfg, args) -> dict:
+    g = cfg.grid
+    return {
+        "workload": (f"{cfg.name}: {cfg.camera.width}x{cfg.camera.height} uint16 depth, "
+                     f"{g.dims[0]}x{g.dims[1]}x{g.dims[2]} TSDF @ {g.voxel_size:g} mm, single-level ICP x10, "
+                     "integration + ray cast per frame"),
+        "tsdf": args.tsdf,
+        "frames_unique": UNIQUE_FRAMES,
+        "l2": f"TSDF {'pair' if args.tsdf == 'f32' else 'half2'} of {g.nvox * (8 if args.tsdf == 'f32' else 4) / 1e6:.0f} MB "
+              "> 129 MB L2 (inputs larger than L2, no flush)",
+        "parallelism": f"replicas x{args.gpus}",
+    }
+
+
+def cpu_baseline(cfg, frames, order, budget_s: float) -> dict:
+    """The reference's kernel bodies compiled for this host's CPU (or the oracle port),
+    frames/s over a bounded sample of the same sequence."""
+    from oracle.pyoracle import GridSpec, Oracle, Reference
+
+    g = cfg.grid
+    gs = GridSpec(tuple(g.dims), tuple(g.start), g.voxel_size)
+    ref = Reference.load()
+    impl, kind = (ref, "reference") if ref is not None else (Oracle(), "port")
+    H, W = cfg.camera.height, cfg.camera.width
+    pipe = impl.pipeline(H, W, gs, cfg.camera.K_reference())
+    pipe.initial(frames[order[0]])
+    n, t0 = 0, time.perf_counter()
+    while n < len(order) - 1:
+        pipe.incoming(frames[order[1 + n]])
+        n += 1
+        if time.perf_counter() - t0 >= budget_s and n >= 2:
+            break
+    dt = time.perf_counter() - t0
+    cores = Oracle().lib.kfo_num_threads()
+    pipe.close()
+    return {"value": n / dt, "unit": "frames/s", "cores": cores, "kind": kind,
+            "sample": f"{n} incoming frames of {cfg.name} after the first, {dt:.1f} s"}
+
+
+def run_reference(args, dist: Dist):
+    cfg = workload(args)
+    if dist.rank != 0:
+        dist.close()
+        return
+    from kinect_fusion_slam_gb300 import scene
+
+    n_frames = min(args.steps + args.warmup + 1, UNIQUE_FRAMES)
+    seq = scene.sequence(cfg, frames=n_frames)
+    frames = seq.depths(n_frames)
+    order = pingpong(n_frames, args.steps + args.warmup + 1)
+    budget = max(10.0, min(120.0, args.cpu_seconds * 4))
+    cb = cpu_baseline(cfg, frames, order, budget)
+    line = {
+        "metric": METRIC, "value": cb["value"], "unit": "frames/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000.0 / cb["value"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic: seeded analytic room, Kinect v1 noise",
+        "config": config_desc(cfg, args), "impl": "reference",
+        "cpu_baseline": {k: cb[k] for k in ("kind", "cores", "sample")} | {"value": cb["value"], "unit": "frames/s"},
+        "e2e": {"value": cb["value"], "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    dist.close()
+
+
+def read_profile_traffic(kernel: str):
+    """Per-launch DRAM bytes of a kernel from the committed ncu summary, if present."""
+    p = ROOT / "profiles" / "ncu_traffic.txt"
+    if not p.exists():
+        return None
+    for line in p.read_text().splitlines():
+        parts = line.split()
+        if len(parts) >= 2 and parts[0] == kernel:
+            try:
+                return float(parts[1])
+            except ValueError:
+                return None
+    return None
+
+
+def run_gb300(args, dist: Dist):
+    import torch
+
+    import kinect_fusion_slam_gb300 as kf
+    from kinect_fusion_slam_gb300 import scene
+
+    torch.cuda.set_device(dist.local_rank)
+    cfg = workload(args)
+    g, cam = cfg.grid, cfg.camera
+    n_total = 1 + args.warmup + args.steps
+    seq = scene.sequence(cfg, frames=UNIQUE_FRAMES)
+    frames = seq.depths(UNIQUE_FRAMES)
+    order = pingpong(UNIQUE_FRAMES, n_total + args.profile_frames + (0 if args.no_e2e else args.steps))
+    K = seq.K
+    storage = kf.KF_TSDF_F16 if args.tsdf == "f16" else kf.KF_TSDF_F32
+    conf = kf.make_config(height=cam.height, width=cam.width, dims=g.dims, grid_start=g.start,
+                          voxel_size=g.voxel_size, tsdf_storage=storage)
+    h = kf.Handle(conf)
+    h.set_intrinsics(K[0, 0], K[1, 1], K[0, 2], K[1, 2])
+    stream = torch.cuda.current_stream()
+    h.set_stream(stream.cuda_stream)
+    dev = torch.from_numpy(frames.view(np.int16)).cuda()
+    fbytes = cam.height * cam.width * 2
+
+    def dptr(k):
+        return dev.data_ptr() + order[k] * fbytes
+
+    h.initial_processing_device(dptr(0))
+    for k in range(1, 1 + args.warmup):
+        h.incoming_frame_device(dptr(k))
+    torch.cuda.synchronize()
+    dist.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(torch.cuda.current_device())
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for k in range(1 + args.warmup, n_total):
+        h.incoming_frame_device(dptr(k))
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    dist.barrier()
+    ms = e0.elapsed_time(e1)
+    ms_max = dist.max(ms)
+    fps = args.steps * dist.world / (ms_max / 1000.0)
+    kpf = h.kernels_per_frame()
+
+    # per-stage device time with CUDA events recorded inside each frame's graph
+    h.enable_stage_timing(True)
+    stages = []
+    for k in range(n_total, n_total + args.profile_frames):
+        h.incoming_frame_device(dptr(k))
+        stages.append(h.stage_times())
+    h.enable_stage_timing(False)
+    st = np.mean(np.array(stages), axis=0) if stages else np.zeros(5)
+    stage_ms = {"vertex": float(st[0]), "icp": float(st[1]), "integration": float(st[2]), "raycast": float(st[3]),
+                "frame": float(st[4])}
+    nc, _ = h.icp_stats(10)
+
+    # end to end through the C ABI with host buffers
+    e2e = None
+    if not args.no_e2e:
+        host = torch.from_numpy(frames.view(np.int16)).pin_memory()
+        base = n_total + args.profile_frames
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for k in range(args.steps):
+            h.incoming_frame_ptr(host.data_ptr() + order[base + k] * fbytes)
+            h.pose()
+        dt = time.perf_counter() - t0
+        dt = dist.max(dt)
+        e2e = {"value": args.steps * dist.world / dt, "unit": "frames/s", "h2d_bytes_per_step": fbytes,
+               "d2h_bytes_per_step": 64}
+
+    # roofline of the dominant stage
+    nvox = g.nvox
+    bpv = 16 if args.tsdf == "f32" else 8
+    dominant = max(("integration", "icp", "raycast"), key=lambda s: stage_ms[s])
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    if dominant == "integration":
+        alg = bpv * nvox
+        kernel = "integrate_kernel"
+    elif dominant == "icp":
+        alg = 49 * cam.height * cam.width * 10
+        kernel = "icp_kernel"
+    else:
+        alg = 4 * 45 * int((frames[0] > 0).sum())
+        kernel = "raycast_kernel"
+    achieved = alg / (stage_ms[dominant] / 1000.0) / 1e9 if stage_ms[dominant] > 0 else 0.0
+    traffic = read_profile_traffic(kernel)
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": traffic, "kernel": kernel, "stage_ms": stage_ms[dominant],
+                "peak_source": "measured" if peaks else "fallback"}
+
+    cb = None
+    if dist.rank == 0 and args.gpus == 1 and not args.no_cpu_baseline:
+        cb = cpu_baseline(cfg, frames, order, args.cpu_seconds)
+
+    line = {
+        "metric": METRIC, "value": fps, "unit": "frames/s", "n_gpus": dist.world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": args.tsdf, "data": "synthetic: seeded analytic room, Kinect v1 noise",
+        "config": config_desc(cfg, args), "roofline": roofline, "cpu_baseline": cb, "e2e": e2e,
+        "gpu_launches": kpf * args.steps, "clocks": clk, "stages_ms": stage_ms,
+        "icp_correspondences_last_frame": [int(x) for x in nc],
+    }
+    h.close()
+    if dist.rank == 0:
+        print(json.dumps(line), flush=True)
+    dist.close()
+
+
+def main(argv=None):
+    args = parse_args(argv)
+    dist = Dist()
+    if args.impl == "reference":
+        run_reference(args, dist)
+    else:
+        run_gb300(args, dist)
+
+
+if __name__ == "__main__":
+    main()

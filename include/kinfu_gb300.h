@@ -1,0 +1,182 @@
+/*
+ * kinfu_gb300 -- C ABI of the GB300 (sm_103a) KinectFusion per-frame path.
+ *
+ * Drop-in for the GPU path of PoChang007/Kinect_Fusion_SLAM: the five extern "C"
+ * launchers of src/parallel_processing/parallel_processing.h:19-53 and the
+ * KinfuPipeline frame loop of src/kinfu_pipeline.{h,cpp}.  Plain pointers and sizes
+ * only; no OpenCV, no CUDA or torch types.
+ *
+ * Conventions (all from the reference):
+ *   - millimetres; 4x4 row-major float camera-to-world pose (kinfu_pipeline.h:18);
+ *   - 1-based pixel coordinates: the principal point is given in the reference's
+ *     convention (cx = 316.625, cy = 256.2318 at kinfu_pipeline.cpp:14-24);
+ *   - images are H x W row-major; the predicted-surface planes are world-space mm
+ *     with 0 where a ray found no surface (kinfu_pipeline.cpp:195-204);
+ *   - volume readback/upload uses the reference's z-fastest order
+ *     idx = x*DY*DZ + y*DZ + z (kinfu_pipeline.cpp:53-55) with NaN = unobserved.
+ *
+ * The library owns all device memory, a CUDA stream and (optionally) captured CUDA
+ * graphs per handle; the caller owns every host buffer.  Every call returns a
+ * kf_status; kf_last_error() gives the message of the handle's latest failure.
+ * A handle must not be used from two threads at once.
+ */
+#ifndef KINFU_GB300_H
+#define KINFU_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int kf_status;
+#define KF_OK 0
+#define KF_ERR_INVALID_ARGUMENT 1
+#define KF_ERR_CUDA 2
+#define KF_ERR_OUT_OF_MEMORY 3
+#define KF_ERR_STATE 4
+#define KF_ERR_IO 5
+#define KF_ERR_UNSUPPORTED 6
+
+/* TSDF storage */
+#define KF_TSDF_F32 0 /* float value + float weight (reference layout and precision) */
+#define KF_TSDF_F16 1 /* half value + half weight pair, 4 bytes per voxel */
+
+/* what an ICP iteration applies when cv::Cholesky would fail (pivot < FLT_EPSILON) */
+#define KF_ICP_FAIL_REFERENCE 0 /* as the reference: the raw A^T b is used as the increment */
+#define KF_ICP_FAIL_IDENTITY 1  /* skip the increment */
+
+/* 6x6 reduction / solve precision */
+#define KF_SOLVE_REFERENCE 0 /* float sums, float-stored Cholesky (cv::Cholesky), float pose */
+#define KF_SOLVE_PRECISE 1   /* compensated float sums, FP64 Cholesky and FP64 pose composition */
+
+typedef struct kf_config {
+    int height, width;       /* depth image size (480, 640: system_interface.cpp:6-7) */
+    float min_depth;         /* mm, inclusive range filter lower bound (300) */
+    float max_depth;         /* mm, inclusive upper bound (2000) */
+    int dims[3];             /* voxel counts x, y, z (360, 360, 300: kinfu_pipeline.h:46-48) */
+    int grid_start[3];       /* integer voxel coordinate of voxel (0,0,0) (-200, -200, -120) */
+    float voxel_size;        /* mm (10) */
+    float truncated_distance;/* mm (300) */
+    float sdf_minimum;       /* mm (-30) */
+    float sdf_maximum;       /* mm (300) */
+    int icp_levels;          /* 1 = single level as the reference; up to 3 (pyramid) */
+    int icp_iterations[3];   /* per level, finest first (10: sensor_pose_estimation.cu:339) */
+    float icp_distance;      /* mm correspondence gate (20: sensor_pose_estimation.cu:48) */
+    float icp_angle_deg;     /* normal gate in degrees (30: sensor_pose_estimation.cu:69) */
+    int icp_fail_mode;       /* KF_ICP_FAIL_* */
+    int solve_mode;          /* KF_SOLVE_* */
+    int tsdf_storage;        /* KF_TSDF_* */
+    int bilateral;           /* 0 = off as in the reference loop (kinfu_pipeline.cpp:141-145) */
+    int bilateral_radius;    /* 3 (kinfu_pipeline.h:58) */
+    float sigma_d;           /* 4.5 (kinfu_pipeline.h:61) */
+    float sigma_r;           /* 30 (kinfu_pipeline.h:62) */
+    int use_graphs;          /* capture the per-frame sequence as CUDA graphs (default 1) */
+} kf_config;
+
+typedef struct kf_handle kf_handle;
+
+/* Reference defaults: 480x640, [300, 2000] mm, 360x360x300 @ 10 mm from (-2000,-2000,
+ * -1200) mm, truncation 300/-30/300, single-level 10-iteration ICP, FP32. */
+void kf_config_default(kf_config* cfg);
+
+/* KinfuPipeline::KinfuPipeline (kinfu_pipeline.cpp:6-65): allocates the device
+ * volume (NaN-filled), sets the reference intrinsics and the identity pose. */
+kf_status kf_create(const kf_config* cfg, kf_handle** out);
+kf_status kf_destroy(kf_handle* h);
+const char* kf_last_error(const kf_handle* h);
+const char* kf_status_string(kf_status s);
+kf_status kf_get_config(const kf_handle* h, kf_config* cfg);
+
+/* intrinsic_matrix (kinfu_pipeline.h:17): fx, fy and the 1-based principal point */
+kf_status kf_set_intrinsics(kf_handle* h, float fx, float fy, float cx, float cy);
+kf_status kf_get_intrinsics(const kf_handle* h, float K[9]);
+/* extrinsic_matrix (kinfu_pipeline.h:18): 4x4 row-major camera-to-world, mm */
+kf_status kf_set_pose(kf_handle* h, const float T[16]);
+kf_status kf_get_pose(kf_handle* h, float T[16]);
+/* resets the volume to NaN and the pose to identity */
+kf_status kf_reset(kf_handle* h);
+
+/* ---- frame loop (KinfuPipeline) --------------------------------------------------
+ * depth: H*W uint16 millimetres (the contents of dep%04d.dat); host pointer, pinned
+ * or pageable.  Range filtering to [min_depth, max_depth] happens on the device. */
+/* InitialProcessing (kinfu_pipeline.cpp:91-119): integrate at the current pose (first
+ * frame semantics) and ray cast the surface prediction */
+kf_status kf_initial_processing(kf_handle* h, const uint16_t* depth);
+/* IncomingFrameProcessing (kinfu_pipeline.cpp:121-193): vertex/normal map, ICP,
+ * integration, ray cast.  Asynchronous on the handle's stream; kf_get_pose or
+ * kf_synchronize waits for it. */
+kf_status kf_incoming_frame(kf_handle* h, const uint16_t* depth);
+/* same as the two above with device-resident input (a device pointer to H*W uint16) */
+kf_status kf_initial_processing_device(kf_handle* h, const uint16_t* depth_dev);
+kf_status kf_incoming_frame_device(kf_handle* h, const uint16_t* depth_dev);
+/* reads dep%04d.dat (system_utility.cpp:58-68) from dir into depth (H*W uint16) */
+kf_status kf_load_depth_dat(const char* dir, int frame_index, int height, int width, uint16_t* depth);
+kf_status kf_synchronize(kf_handle* h);
+/* run the handle's work on a caller-owned cudaStream_t (passed as void*); NULL goes
+ * back to the handle's own stream.  Captured graphs are launched on whichever stream
+ * is current. */
+kf_status kf_set_stream(kf_handle* h, void* stream);
+
+/* ray_casting_data->surface_prediction_{x,y,z} and surface_prediction_normal_{x,y,z}
+ * (system_utility.h:26-35): six H*W host planes; any pointer may be NULL */
+kf_status kf_get_predicted(kf_handle* h, float* x, float* y, float* z, float* nx, float* ny, float* nz);
+/* global_tsdf / global_weight_tsdf (kinfu_pipeline.h:24-25) in the reference's order;
+ * either pointer may be NULL */
+kf_status kf_get_volume(kf_handle* h, float* tsdf, float* weight);
+kf_status kf_set_volume(kf_handle* h, const float* tsdf, const float* weight);
+/* the range-filtered float depth of the latest frame (depth_image_next) */
+kf_status kf_get_depth(kf_handle* h, float* depth);
+/* per-iteration ICP log of the latest frame: correspondences, whether the Cholesky
+ * factorisation succeeded, and the pose after the iteration (16 floats each); n =
+ * number of iterations the arrays hold; any pointer may be NULL */
+kf_status kf_get_icp_stats(kf_handle* h, int32_t* ncorr, int32_t* chol_ok, float* poses, int n);
+
+/* ---- stage launchers (parallel_processing.h:19-53), on the handle's device state --
+ * Each runs one stage on the depth / pose / prediction the handle holds. */
+/* depth input as float (the reference passes cv::Mat CV_32F); no range filter */
+kf_status kf_set_depth_f32(kf_handle* h, const float* depth);
+/* uint16 input with the range filter (LoadDepthData + GetRangeDepth) */
+kf_status kf_set_depth_u16(kf_handle* h, const uint16_t* depth);
+/* Calculate_Vertices_And_Normals (raw_vertices.cu:53): outputs may be NULL */
+kf_status kf_calculate_vertices_and_normals(kf_handle* h, float* vx, float* vy, float* nx, float* ny, float* nz,
+                                            uint8_t* mask);
+/* Bilateral_Filtering (bilateral_filtering.cu:49): filters the held depth in place */
+kf_status kf_bilateral_filtering(kf_handle* h);
+/* Estimate_Sensor_Pose (sensor_pose_estimation.cu:247): ICP from the held vertex map
+ * against the held prediction; updates the pose */
+kf_status kf_estimate_sensor_pose(kf_handle* h);
+/* Projective_TSDF (projective_tsdf.cu:142): integrates the held depth at the pose */
+kf_status kf_projective_tsdf(kf_handle* h, int first_tsdf_construct);
+/* Ray_Casting (voxel_traversal.cu:426): predicts the surface from the held depth at the
+ * pose; hit (may be NULL) receives the z-fastest index of the zero-crossing voxel or -1 */
+kf_status kf_ray_casting(kf_handle* h, int32_t* hit);
+
+/* ---- parity hooks --------------------------------------------------------------- */
+/* replaces the held prediction (six H*W planes, as kf_get_predicted) */
+kf_status kf_set_predicted(kf_handle* h, const float* x, const float* y, const float* z, const float* nx,
+                           const float* ny, const float* nz);
+/* one ICP association + reduction at the given frame-to-frame F and pose T without
+ * updating anything: pair[i] = matched pixel index or -1 (may be NULL), sums27 = the 6
+ * entries of A^T b then the 21 of the upper triangle of A^T A, row by row; returns the
+ * correspondence count in *ncorr */
+kf_status kf_icp_associate(kf_handle* h, const float F[16], const float T[16], int32_t* pair, float* sums27,
+                           int32_t* ncorr);
+/* the float below which the ray-cast normal is flipped (voxel_traversal.cu:361-369),
+ * computed on the device from its own acos at kf_create */
+kf_status kf_get_flip_threshold(kf_handle* h, float* c_flip);
+
+/* ---- timing --------------------------------------------------------------------- */
+/* per-stage device time of the latest kf_incoming_frame (CUDA events, ms):
+ * [0] depth+vertex, [1] ICP, [2] integration, [3] ray cast, [4] whole frame.
+ * Collected only while enabled (it splits the frame's graph into stages). */
+kf_status kf_enable_stage_timing(kf_handle* h, int enable);
+kf_status kf_get_stage_times(kf_handle* h, float ms[5]);
+/* number of kernels one kf_incoming_frame launches */
+kf_status kf_kernels_per_frame(kf_handle* h, int* n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,891 @@
+// C ABI of the kinfu_gb300 library (include/kinfu_gb300.h).
+//
+// A handle owns the device-resident state of one KinfuPipeline: the volume, the
+// depth / vertex / prediction images, the pose and ICP scratch in a State block, a
+// CUDA stream and, optionally, the per-frame kernel sequence captured as CUDA graphs.
+// The pose never leaves the device during a frame: every kernel reads it from, and
+// the ICP's last block writes it to, the State block.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/kinfu_gb300.h"
+#include "kf_kernels.h"
+
+using namespace kf;
+
+struct kf_handle {
+    kf_config cfg{};
+    Grid grid{};
+    Camera cam{};
+    IcpParams icp{};
+    int device = 0;
+    cudaStream_t stream = nullptr;      // stream all work goes to
+    cudaStream_t own_stream = nullptr;  // the handle's own stream
+    size_t nvox = 0;
+    long long skip_from = 0;  // first z-fastest voxel index the reference never integrates
+
+    uint16_t* d_raw = nullptr;
+    float* d_depth = nullptr;
+    float* d_depth_tmp = nullptr;  // bilateral output
+    float4 *d_vmap = nullptr, *d_nmap = nullptr, *d_pv = nullptr, *d_pn = nullptr;
+    int32_t* d_hit = nullptr;
+    int32_t* d_pair = nullptr;
+    float2* d_tab = nullptr;
+    float* d_tsdf = nullptr;
+    float* d_weight = nullptr;
+    __half2* d_vol16 = nullptr;
+    State* d_state = nullptr;
+    float* d_partials = nullptr;
+    float* d_mats = nullptr;  // F, T (debug association input) + sums output
+    float* d_spatial = nullptr;
+
+    uint16_t* h_raw = nullptr;  // pinned staging for pageable host input
+    State* h_state = nullptr;   // pinned readback
+
+    cudaGraphExec_t g_incoming = nullptr, g_initial = nullptr;
+    bool timing = false;
+    cudaEvent_t ev[5] = {};
+    float stage_ms[5] = {};
+    bool frame_timed = false;
+    std::string err;
+};
+
+namespace {
+
+kf_status fail(kf_handle* h, kf_status s, const std::string& msg)
+{
+    if (h) h->err = msg;
+    return s;
+}
+
+#define KF_CUDA(h, call)                                                                                  \
+    do {                                                                                                  \
+        cudaError_t e_ = (call);                                                                          \
+        if (e_ != cudaSuccess) {                                                                          \
+            return fail((h), e_ == cudaErrorMemoryAllocation ? KF_ERR_OUT_OF_MEMORY : KF_ERR_CUDA,        \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));                              \
+        }                                                                                                 \
+    } while (0)
+
+#define KF_CHECK_LAUNCH(h) KF_CUDA(h, cudaGetLastError())
+
+template <class T>
+T* field_ptr(State* st, size_t offset)
+{
+    return reinterpret_cast<T*>(reinterpret_cast<char*>(st) + offset);
+}
+
+void destroy_graphs(kf_handle* h)
+{
+    if (h->g_incoming) cudaGraphExecDestroy(h->g_incoming);
+    if (h->g_initial) cudaGraphExecDestroy(h->g_initial);
+    h->g_incoming = h->g_initial = nullptr;
+}
+
+bool validate(const kf_config* c, std::string& why)
+{
+    if (c->height < 2 || c->width < 2 || (long long)c->height * c->width > (1LL << 26)) {
+        why = "image size out of range";
+        return false;
+    }
+    for (int k = 0; k < 3; ++k)
+        if (c->dims[k] < 3 || c->dims[k] > 4096) {
+            why = "grid dimensions out of range";
+            return false;
+        }
+    if ((double)c->dims[0] * c->dims[1] * c->dims[2] > 2147483647.0) {
+        why = "grid has more than 2^31-1 voxels (the reference indexes voxels with int)";
+        return false;
+    }
+    if (!(c->voxel_size > 0) || !(c->truncated_distance > 0)) {
+        why = "voxel_size and truncated_distance must be positive";
+        return false;
+    }
+    if (c->icp_levels != 1) {
+        why = "only single-level ICP is implemented (icp_levels must be 1)";
+        return false;
+    }
+    if (c->icp_iterations[0] < 0 || c->icp_iterations[0] > kMaxIcpIters) {
+        why = "icp_iterations out of range [0, 64]";
+        return false;
+    }
+    if (c->tsdf_storage != KF_TSDF_F32 && c->tsdf_storage != KF_TSDF_F16) {
+        why = "unknown tsdf_storage";
+        return false;
+    }
+    if (c->bilateral_radius < 1 || c->bilateral_radius > 7) {
+        why = "bilateral_radius must be in [1, 7]";
+        return false;
+    }
+    return true;
+}
+
+// smallest z-fastest index i with (float)i >= (float)DX * (float)DY * (float)DZ: the
+// reference kernel's guard (projective_tsdf.cu:14) returns for these threads
+long long float_guard_start(const int* d)
+{
+    const float nf = (float)d[0] * (float)d[1] * (float)d[2];
+    long long n = (long long)d[0] * d[1] * d[2];
+    long long i = n;
+    while (i > 0 && (float)(i - 1) >= nf) --i;
+    return i;
+}
+
+kf_status upload_raw(kf_handle* h, const uint16_t* depth)
+{
+    const size_t bytes = sizeof(uint16_t) * h->cam.H * h->cam.W;
+    cudaPointerAttributes attr{};
+    const bool pinned = cudaPointerGetAttributes(&attr, depth) == cudaSuccess &&
+                        (attr.type == cudaMemoryTypeHost || attr.type == cudaMemoryTypeManaged);
+    cudaGetLastError();
+    if (pinned) {
+        KF_CUDA(h, cudaMemcpyAsync(h->d_raw, depth, bytes, cudaMemcpyHostToDevice, h->stream));
+    } else {
+        // the staging buffer may still feed an earlier copy
+        KF_CUDA(h, cudaStreamSynchronize(h->stream));
+        std::memcpy(h->h_raw, depth, bytes);
+        KF_CUDA(h, cudaMemcpyAsync(h->d_raw, h->h_raw, bytes, cudaMemcpyHostToDevice, h->stream));
+    }
+    return KF_OK;
+}
+
+// ---- stage enqueuers (no synchronisation) ----
+void enq_ingest(kf_handle* h, const uint16_t* raw, bool init_icp, bool normals)
+{
+    launch_vertex(raw, h->d_depth, h->d_vmap, h->d_nmap, h->cam, h->cfg.min_depth, h->cfg.max_depth, h->d_state,
+                  init_icp, normals, h->stream);
+}
+
+void enq_bilateral(kf_handle* h)
+{
+    launch_bilateral(h->d_depth, h->d_depth_tmp, h->d_spatial, h->cfg.bilateral_radius, h->cfg.sigma_r, h->cam.H,
+                     h->cam.W, h->stream);
+    cudaMemcpyAsync(h->d_depth, h->d_depth_tmp, sizeof(float) * h->cam.H * h->cam.W, cudaMemcpyDeviceToDevice,
+                    h->stream);
+}
+
+void enq_icp(kf_handle* h)
+{
+    for (int it = 0; it < h->cfg.icp_iterations[0]; ++it)
+        launch_icp_iteration(h->d_vmap, h->d_nmap, h->d_pv, h->d_pn, h->cam, h->icp, h->d_state, h->d_partials,
+                             h->stream);
+}
+
+void enq_integrate(kf_handle* h, bool first)
+{
+    launch_integrate_prep(h->d_depth, h->d_tab, h->cam, h->d_state, h->stream);
+    if (h->d_vol16)
+        launch_integrate_f16(h->d_vol16, h->d_tab, h->d_state, h->grid, h->cam, h->skip_from, first, h->stream);
+    else
+        launch_integrate_f32(h->d_tsdf, h->d_weight, h->d_tab, h->d_state, h->grid, h->cam, h->skip_from, first,
+                             h->stream);
+}
+
+void enq_raycast(kf_handle* h, int32_t* hit)
+{
+    if (h->d_vol16)
+        launch_raycast_f16(h->d_vol16, h->d_depth, h->d_pv, h->d_pn, hit, h->cam, h->grid, h->d_state, h->stream);
+    else
+        launch_raycast_f32(h->d_tsdf, h->d_depth, h->d_pv, h->d_pn, hit, h->cam, h->grid, h->d_state, h->stream);
+}
+
+// stage timing event k; inside a stream capture the record must be an external
+// event node to fire when the graph is replayed
+void stamp(kf_handle* h, int k)
+{
+    if (!h->timing) return;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaStreamIsCapturing(h->stream, &cs);
+    if (cs == cudaStreamCaptureStatusActive)
+        cudaEventRecordWithFlags(h->ev[k], h->stream, cudaEventRecordExternal);
+    else
+        cudaEventRecord(h->ev[k], h->stream);
+}
+
+// IncomingFrameProcessing after the depth upload (kinfu_pipeline.cpp:128-188).  The
+// bilateral call site the reference leaves commented out sits after the vertex map
+// (kinfu_pipeline.cpp:141-145): when enabled here it filters the depth that ICP,
+// integration and ray casting use, in the same place.
+void enq_incoming(kf_handle* h, const uint16_t* raw)
+{
+    stamp(h, 0);
+    enq_ingest(h, raw, true, true);
+    if (h->cfg.bilateral) enq_bilateral(h);
+    stamp(h, 1);
+    enq_icp(h);
+    stamp(h, 2);
+    enq_integrate(h, false);
+    stamp(h, 3);
+    enq_raycast(h, h->d_hit);
+    stamp(h, 4);
+}
+
+// InitialProcessing after the depth upload (kinfu_pipeline.cpp:93-115)
+void enq_initial(kf_handle* h, const uint16_t* raw)
+{
+    enq_ingest(h, raw, false, true);
+    enq_integrate(h, true);
+    enq_raycast(h, h->d_hit);
+}
+
+kf_status run_captured(kf_handle* h, cudaGraphExec_t& exec, bool incoming)
+{
+    if (!h->cfg.use_graphs) {
+        if (incoming)
+            enq_incoming(h, h->d_raw);
+        else
+            enq_initial(h, h->d_raw);
+        KF_CHECK_LAUNCH(h);
+        return KF_OK;
+    }
+    if (!exec) {
+        cudaGraph_t graph = nullptr;
+        KF_CUDA(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+        if (incoming)
+            enq_incoming(h, h->d_raw);
+        else
+            enq_initial(h, h->d_raw);
+        cudaError_t le = cudaGetLastError();
+        cudaError_t ce = cudaStreamEndCapture(h->stream, &graph);
+        if (le != cudaSuccess || ce != cudaSuccess) {
+            if (graph) cudaGraphDestroy(graph);
+            return fail(h, KF_ERR_CUDA,
+                        std::string("graph capture failed: ") + cudaGetErrorString(le != cudaSuccess ? le : ce));
+        }
+        cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ie != cudaSuccess) {
+            exec = nullptr;
+            return fail(h, KF_ERR_CUDA, std::string("graph instantiate failed: ") + cudaGetErrorString(ie));
+        }
+    }
+    KF_CUDA(h, cudaGraphLaunch(exec, h->stream));
+    return KF_OK;
+}
+
+kf_status read_state(kf_handle* h)
+{
+    KF_CUDA(h, cudaMemcpyAsync(h->h_state, h->d_state, sizeof(State), cudaMemcpyDeviceToHost, h->stream));
+    KF_CUDA(h, cudaStreamSynchronize(h->stream));
+    return KF_OK;
+}
+
+void set_camera(kf_handle* h, float fx, float fy, float cx, float cy)
+{
+    float K[9] = {fx, 0.0f, cx, 0.0f, fy, cy, 0.0f, 0.0f, 1.0f};
+    std::memcpy(h->cam.K, K, sizeof(K));
+    inv3(h->cam.K, h->cam.Ki);
+}
+
+template <class T>
+kf_status dalloc(kf_handle* h, T** p, size_t count)
+{
+    KF_CUDA(h, cudaMalloc((void**)p, sizeof(T) * (count ? count : 1)));
+    return KF_OK;
+}
+
+#define KF_TRY(expr)                      \
+    do {                                  \
+        kf_status s_ = (expr);            \
+        if (s_ != KF_OK) return s_;       \
+    } while (0)
+
+#define KF_HANDLE(h)                                    \
+    do {                                                \
+        if (!(h)) return KF_ERR_INVALID_ARGUMENT;       \
+        cudaSetDevice((h)->device);                     \
+    } while (0)
+
+kf_status allocate(kf_handle* h)
+{
+    const size_t HW = (size_t)h->cam.H * h->cam.W;
+    KF_TRY(dalloc(h, &h->d_raw, HW));
+    KF_TRY(dalloc(h, &h->d_depth, HW));
+    KF_TRY(dalloc(h, &h->d_depth_tmp, HW));
+    KF_TRY(dalloc(h, &h->d_vmap, HW));
+    KF_TRY(dalloc(h, &h->d_nmap, HW));
+    KF_TRY(dalloc(h, &h->d_pv, HW));
+    KF_TRY(dalloc(h, &h->d_pn, HW));
+    KF_TRY(dalloc(h, &h->d_hit, HW));
+    KF_TRY(dalloc(h, &h->d_pair, HW));
+    KF_TRY(dalloc(h, &h->d_tab, HW));
+    KF_TRY(dalloc(h, &h->d_state, 1));
+    KF_TRY(dalloc(h, &h->d_partials, (size_t)2 * icp_grid_blocks(h->cam.H, h->cam.W) * kIcpVals));
+    KF_TRY(dalloc(h, &h->d_mats, 64));
+    KF_TRY(dalloc(h, &h->d_spatial, 15 * 15));
+    if (h->cfg.tsdf_storage == KF_TSDF_F16) {
+        KF_TRY(dalloc(h, &h->d_vol16, h->nvox));
+    } else {
+        KF_TRY(dalloc(h, &h->d_tsdf, h->nvox));
+        KF_TRY(dalloc(h, &h->d_weight, h->nvox));
+    }
+    KF_CUDA(h, cudaMallocHost((void**)&h->h_raw, sizeof(uint16_t) * HW));
+    KF_CUDA(h, cudaMallocHost((void**)&h->h_state, sizeof(State)));
+    for (auto& e : h->ev) KF_CUDA(h, cudaEventCreate(&e));
+    return KF_OK;
+}
+
+kf_status reset_state(kf_handle* h)
+{
+    const size_t HW = (size_t)h->cam.H * h->cam.W;
+    if (h->d_vol16)
+        launch_fill_nan_half2(h->d_vol16, h->nvox, h->stream);
+    else {
+        launch_fill_nan(h->d_tsdf, h->nvox, h->stream);
+        launch_fill_nan(h->d_weight, h->nvox, h->stream);
+    }
+    KF_CHECK_LAUNCH(h);
+    KF_CUDA(h, cudaMemsetAsync(h->d_depth, 0, sizeof(float) * HW, h->stream));
+    KF_CUDA(h, cudaMemsetAsync(h->d_vmap, 0, sizeof(float4) * HW, h->stream));
+    KF_CUDA(h, cudaMemsetAsync(h->d_nmap, 0, sizeof(float4) * HW, h->stream));
+    KF_CUDA(h, cudaMemsetAsync(h->d_pv, 0, sizeof(float4) * HW, h->stream));
+    KF_CUDA(h, cudaMemsetAsync(h->d_pn, 0, sizeof(float4) * HW, h->stream));
+    KF_CUDA(h, cudaMemsetAsync(h->d_hit, 0xff, sizeof(int32_t) * HW, h->stream));
+    std::memset(h->h_state, 0, sizeof(State));
+    for (int k = 0; k < 16; ++k) {
+        h->h_state->T[k] = (k % 5 == 0) ? 1.f : 0.f;
+        h->h_state->Td[k] = (k % 5 == 0) ? 1.0 : 0.0;
+    }
+    KF_CUDA(h, cudaMemcpyAsync(h->d_state, h->h_state, sizeof(State), cudaMemcpyHostToDevice, h->stream));
+    launch_calibrate(h->d_state, h->stream);
+    KF_CHECK_LAUNCH(h);
+    KF_CUDA(h, cudaStreamSynchronize(h->stream));
+    return KF_OK;
+}
+
+void free_all(kf_handle* h)
+{
+    destroy_graphs(h);
+    void* dev[] = {h->d_raw, h->d_depth, h->d_depth_tmp, h->d_vmap, h->d_nmap, h->d_pv, h->d_pn, h->d_hit,
+                   h->d_pair, h->d_tab, h->d_tsdf, h->d_weight, h->d_vol16, h->d_state, h->d_partials, h->d_mats,
+                   h->d_spatial};
+    for (void* p : dev)
+        if (p) cudaFree(p);
+    if (h->h_raw) cudaFreeHost(h->h_raw);
+    if (h->h_state) cudaFreeHost(h->h_state);
+    for (auto& e : h->ev)
+        if (e) cudaEventDestroy(e);
+    if (h->own_stream) cudaStreamDestroy(h->own_stream);
+}
+
+kf_status upload_spatial(kf_handle* h)
+{
+    // SystemUtility::CreateSpatialKernel + GaussianDistanceWeight
+    // (system_utility.cpp:94-113): exp(-(dx^2 + dy^2) / (2 sigma_d^2)), row = dy
+    const int r = h->cfg.bilateral_radius, kl = 2 * r + 1;
+    std::vector<float> w((size_t)kl * kl);
+    for (int y = -r; y <= r; ++y)
+        for (int x = -r; x <= r; ++x) {
+            const float e = -((float)(x * x) + (float)(y * y)) / (2 * h->cfg.sigma_d * h->cfg.sigma_d);
+            w[(y + r) * kl + (x + r)] = (float)std::exp((double)e);
+        }
+    KF_CUDA(h, cudaMemcpy(h->d_spatial, w.data(), sizeof(float) * w.size(), cudaMemcpyHostToDevice));
+    return KF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void kf_config_default(kf_config* c)
+{
+    if (!c) return;
+    std::memset(c, 0, sizeof(*c));
+    c->height = 480;
+    c->width = 640;
+    c->min_depth = 300.f;
+    c->max_depth = 2000.f;
+    c->dims[0] = 360;
+    c->dims[1] = 360;
+    c->dims[2] = 300;
+    c->grid_start[0] = -200;
+    c->grid_start[1] = -200;
+    c->grid_start[2] = -120;
+    c->voxel_size = 10.f;
+    c->truncated_distance = 300.f;
+    c->sdf_minimum = -30.f;
+    c->sdf_maximum = 300.f;
+    c->icp_levels = 1;
+    c->icp_iterations[0] = 10;
+    c->icp_distance = 20.f;
+    c->icp_angle_deg = 30.f;
+    c->icp_fail_mode = KF_ICP_FAIL_REFERENCE;
+    c->solve_mode = KF_SOLVE_REFERENCE;
+    c->tsdf_storage = KF_TSDF_F32;
+    c->bilateral = 0;
+    c->bilateral_radius = 3;
+    c->sigma_d = 4.5f;
+    c->sigma_r = 30.f;
+    c->use_graphs = 1;
+}
+
+const char* kf_status_string(kf_status s)
+{
+    switch (s) {
+    case KF_OK: return "ok";
+    case KF_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case KF_ERR_CUDA: return "CUDA error";
+    case KF_ERR_OUT_OF_MEMORY: return "out of device memory";
+    case KF_ERR_STATE: return "invalid state";
+    case KF_ERR_IO: return "I/O error";
+    case KF_ERR_UNSUPPORTED: return "unsupported";
+    default: return "unknown status";
+    }
+}
+
+kf_status kf_create(const kf_config* cfg, kf_handle** out)
+{
+    if (!cfg || !out) return KF_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    std::string why;
+    if (!validate(cfg, why)) return KF_ERR_INVALID_ARGUMENT;
+    kf_handle* h = new kf_handle;
+    h->cfg = *cfg;
+    cudaGetDevice(&h->device);
+    h->grid = Grid{cfg->dims[0], cfg->dims[1], cfg->dims[2], cfg->grid_start[0], cfg->grid_start[1],
+                   cfg->grid_start[2], cfg->voxel_size, cfg->truncated_distance, cfg->sdf_minimum, cfg->sdf_maximum};
+    h->cam.H = cfg->height;
+    h->cam.W = cfg->width;
+    // the reference's intrinsics (kinfu_pipeline.cpp:14-24)
+    set_camera(h, 524.639f, 523.503f, 316.625f, 256.2318f);
+    h->icp = IcpParams{cfg->icp_distance, cfg->icp_angle_deg, cfg->icp_fail_mode,
+                       cfg->solve_mode == KF_SOLVE_PRECISE ? 1 : 0};
+    h->nvox = (size_t)cfg->dims[0] * cfg->dims[1] * cfg->dims[2];
+    h->skip_from = float_guard_start(cfg->dims);
+    kf_status s = KF_OK;
+    if (cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking) != cudaSuccess) s = KF_ERR_CUDA;
+    h->stream = h->own_stream;
+    if (s == KF_OK) s = allocate(h);
+    if (s == KF_OK && cfg->bilateral) s = upload_spatial(h);
+    if (s == KF_OK) s = reset_state(h);
+    if (s != KF_OK) {
+        free_all(h);
+        delete h;
+        return s;
+    }
+    *out = h;
+    return KF_OK;
+}
+
+kf_status kf_destroy(kf_handle* h)
+{
+    if (!h) return KF_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(h->device);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    free_all(h);
+    delete h;
+    return KF_OK;
+}
+
+const char* kf_last_error(const kf_handle* h) { return h ? h->err.c_str() : "null handle"; }
+
+kf_status kf_get_config(const kf_handle* h, kf_config* cfg)
+{
+    if (!h || !cfg) return KF_ERR_INVALID_ARGUMENT;
+    *cfg = h->cfg;
+    return KF_OK;
+}
+
+kf_status kf_set_intrinsics(kf_handle* h, float fx, float fy, float cx, float cy)
+{
+    KF_HANDLE(h);
+    if (!(fx > 0) || !(fy > 0) || !std::isfinite(cx) || !std::isfinite(cy))
+        return fail(h, KF_ERR_INVALID_ARGUMENT, "intrinsics must be finite with positive focal lengths");
+    KF_CUDA(h, cudaStreamSynchronize(h->stream));
+    set_camera(h, fx, fy, cx, cy);
+    destroy_graphs(h);  // the intrinsics are kernel arguments baked into the graphs
+    return KF_OK;
+}
+
+kf_status kf_get_intrinsics(const kf_handle* h, float K[9])
+{
+    if (!h || !K) return KF_ERR_INVALID_ARGUMENT;
+    std::memcpy(K, h->cam.K, sizeof(float) * 9);
+    return KF_OK;
+}
+
+kf_status kf_set_pose(kf_handle* h, const float T[16])
+{
+    KF_HANDLE(h);
+    if (!T) return fail(h, KF_ERR_INVALID_ARGUMENT, "null pose");
+    for (int k = 0; k < 16; ++k)
+        if (!std::isfinite(T[k])) return fail(h, KF_ERR_INVALID_ARGUMENT, "pose has a non-finite entry");
+    KF_CUDA(h, cudaStreamSynchronize(h->stream));
+    std::memcpy(h->h_state->T, T, sizeof(float) * 16);
+    for (int k = 0; k < 16; ++k) h->h_state->Td[k] = (double)T[k];
+    KF_CUDA(h, cudaMemcpyAsync(field_ptr<float>(h->d_state, offsetof(State, T)), h->h_state->T, sizeof(float) * 16,
+                               cudaMemcpyHostToDevice, h->stream));
+    KF_CUDA(h, cudaMemcpyAsync(field_ptr<double>(h->d_state, offsetof(State, Td)), h->h_state->Td,
+                               sizeof(double) * 16, cudaMemcpyHostToDevice, h->stream));
+    KF_CUDA(h, cudaStreamSynchronize(h->stream));
+    return KF_OK;
+}
+
+kf_status kf_get_pose(kf_handle* h, float T[16])
+{
+    KF_HANDLE(h);
+    if (!T) return fail(h, KF_ERR_INVALID_ARGUMENT, "null pose");
+    KF_CUDA(h, cudaMemcpyAsync(T, field_ptr<float>(h->d_state, offsetof(State, T)), sizeof(float) * 16,
+                               cudaMemcpyDeviceToHost, h->stream));
+    KF_CUDA(h, cudaStreamSynchronize(h->stream));
+    return KF_OK;
+}
+
+kf_status kf_reset(kf_handle* h)
+{
+    KF_HANDLE(h);
+    KF_CUDA(h, cudaStreamSynchronize(h->stream));
+    return reset_state(h);
+}
+
+kf_status kf_synchronize(kf_handle* h)
+{
+    KF_HANDLE(h);
+    KF_CUDA(h, cudaStreamSynchronize(h->stream));
+    if (h->frame_timed) {
+        h->frame_timed = false;
+        for (int k = 0; k < 4; ++k) cudaEventElapsedTime(&h->stage_ms[k], h->ev[k], h->ev[k + 1]);
+        cudaEventElapsedTime(&h->stage_ms[4], h->ev[0], h->ev[4]);
+    }
+    return KF_OK;
+}
+
+kf_status kf_set_stream(kf_handle* h, void* stream)
+{
+    KF_HANDLE(h);
+    KF_CUDA(h, cudaStreamSynchronize(h->stream));
+    h->stream = stream ? static_cast<cudaStream_t>(stream) : h->own_stream;
+    return KF_OK;
+}
+
+kf_status kf_initial_processing(kf_handle* h, const uint16_t* depth)
+{
+    KF_HANDLE(h);
+    if (!depth) return fail(h, KF_ERR_INVALID_ARGUMENT, "null depth");
+    KF_TRY(upload_raw(h, depth));
+    KF_TRY(run_captured(h, h->g_initial, false));
+    return KF_OK;
+}
+
+kf_status kf_incoming_frame(kf_handle* h, const uint16_t* depth)
+{
+    KF_HANDLE(h);
+    if (!depth) return fail(h, KF_ERR_INVALID_ARGUMENT, "null depth");
+    KF_TRY(upload_raw(h, depth));
+    KF_TRY(run_captured(h, h->g_incoming, true));
+    h->frame_timed = h->timing;
+    return KF_OK;
+}
+
+kf_status kf_initial_processing_device(kf_handle* h, const uint16_t* depth_dev)
+{
+    KF_HANDLE(h);
+    if (!depth_dev) return fail(h, KF_ERR_INVALID_ARGUMENT, "null depth");
+    KF_CUDA(h, cudaMemcpyAsync(h->d_raw, depth_dev, sizeof(uint16_t) * h->cam.H * h->cam.W, cudaMemcpyDeviceToDevice,
+                               h->stream));
+    KF_TRY(run_captured(h, h->g_initial, false));
+    return KF_OK;
+}
+
+kf_status kf_incoming_frame_device(kf_handle* h, const uint16_t* depth_dev)
+{
+    KF_HANDLE(h);
+    if (!depth_dev) return fail(h, KF_ERR_INVALID_ARGUMENT, "null depth");
+    KF_CUDA(h, cudaMemcpyAsync(h->d_raw, depth_dev, sizeof(uint16_t) * h->cam.H * h->cam.W, cudaMemcpyDeviceToDevice,
+                               h->stream));
+    KF_TRY(run_captured(h, h->g_incoming, true));
+    h->frame_timed = h->timing;
+    return KF_OK;
+}
+
+kf_status kf_load_depth_dat(const char* dir, int frame_index, int height, int width, uint16_t* depth)
+{
+    if (!dir || !depth || height <= 0 || width <= 0) return KF_ERR_INVALID_ARGUMENT;
+    char path[4096];
+    std::snprintf(path, sizeof(path), "%s/dep%04d.dat", dir, frame_index);
+    FILE* fp = std::fopen(path, "rb");
+    if (!fp) return KF_ERR_IO;
+    const size_t n = (size_t)height * width;
+    const size_t got = std::fread(depth, sizeof(uint16_t), n, fp);
+    std::fclose(fp);
+    return got == n ? KF_OK : KF_ERR_IO;
+}
+
+kf_status kf_get_predicted(kf_handle* h, float* x, float* y, float* z, float* nx, float* ny, float* nz)
+{
+    KF_HANDLE(h);
+    const size_t HW = (size_t)h->cam.H * h->cam.W;
+    std::vector<float4> pv(HW), pn(HW);
+    KF_CUDA(h, cudaMemcpyAsync(pv.data(), h->d_pv, sizeof(float4) * HW, cudaMemcpyDeviceToHost, h->stream));
+    KF_CUDA(h, cudaMemcpyAsync(pn.data(), h->d_pn, sizeof(float4) * HW, cudaMemcpyDeviceToHost, h->stream));
+    KF_CUDA(h, cudaStreamSynchronize(h->stream));
+    for (size_t i = 0; i < HW; ++i) {
+        if (x) x[i] = pv[i].x;
+        if (y) y[i] = pv[i].y;
+        if (z) z[i] = pv[i].z;
+        if (nx) nx[i] = pn[i].x;
+        if (ny) ny[i] = pn[i].y;
+        if (nz) nz[i] = pn[i].z;
+    }
+    return KF_OK;
+}
+
+kf_status kf_set_predicted(kf_handle* h, const float* x, const float* y, const float* z, const float* nx,
+                           const float* ny, const float* nz)
+{
+    KF_HANDLE(h);
+    if (!x || !y || !z || !nx || !ny || !nz) return fail(h, KF_ERR_INVALID_ARGUMENT, "null plane");
+    const size_t HW = (size_t)h->cam.H * h->cam.W;
+    std::vector<float4> pv(HW), pn(HW);
+    for (size_t i = 0; i < HW; ++i) {
+        pv[i] = make_float4(x[i], y[i], z[i], 0.f);
+        pn[i] = make_float4(nx[i], ny[i], nz[i], 0.f);
+    }
+    KF_CUDA(h, cudaMemcpyAsync(h->d_pv, pv.data(), sizeof(float4) * HW, cudaMemcpyHostToDevice, h->stream));
+    KF_CUDA(h, cudaMemcpyAsync(h->d_pn, pn.data(), sizeof(float4) * HW, cudaMemcpyHostToDevice, h->stream));
+    KF_CUDA(h, cudaStreamSynchronize(h->stream));
+    return KF_OK;
+}
+
+kf_status kf_get_volume(kf_handle* h, float* tsdf, float* weight)
+{
+    KF_HANDLE(h);
+    float *dt = nullptr, *dw = nullptr;
+    KF_CUDA(h, cudaMalloc((void**)&dt, sizeof(float) * h->nvox));
+    cudaError_t e = cudaMalloc((void**)&dw, sizeof(float) * h->nvox);
+    if (e != cudaSuccess) {
+        cudaFree(dt);
+        return fail(h, KF_ERR_OUT_OF_MEMORY, "volume readback buffer");
+    }
+    if (h->d_vol16) {
+        launch_half2_to_zfast(h->d_vol16, dt, dw, h->grid, h->stream);
+    } else {
+        launch_to_zfast_f32(h->d_tsdf, dt, h->grid, h->stream);
+        launch_to_zfast_f32(h->d_weight, dw, h->grid, h->stream);
+    }
+    e = cudaGetLastError();
+    if (e == cudaSuccess && tsdf)
+        e = cudaMemcpyAsync(tsdf, dt, sizeof(float) * h->nvox, cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess && weight)
+        e = cudaMemcpyAsync(weight, dw, sizeof(float) * h->nvox, cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    cudaFree(dt);
+    cudaFree(dw);
+    if (e != cudaSuccess) return fail(h, KF_ERR_CUDA, std::string("kf_get_volume: ") + cudaGetErrorString(e));
+    return KF_OK;
+}
+
+kf_status kf_set_volume(kf_handle* h, const float* tsdf, const float* weight)
+{
+    KF_HANDLE(h);
+    if (!tsdf || !weight) return fail(h, KF_ERR_INVALID_ARGUMENT, "null volume");
+    float *dt = nullptr, *dw = nullptr;
+    KF_CUDA(h, cudaMalloc((void**)&dt, sizeof(float) * h->nvox));
+    cudaError_t e = cudaMalloc((void**)&dw, sizeof(float) * h->nvox);
+    if (e != cudaSuccess) {
+        cudaFree(dt);
+        return fail(h, KF_ERR_OUT_OF_MEMORY, "volume upload buffer");
+    }
+    e = cudaMemcpyAsync(dt, tsdf, sizeof(float) * h->nvox, cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dw, weight, sizeof(float) * h->nvox, cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess) {
+        if (h->d_vol16) {
+            launch_zfast_to_half2(dt, dw, h->d_vol16, h->grid, h->stream);
+        } else {
+            launch_from_zfast_f32(dt, h->d_tsdf, h->grid, h->stream);
+            launch_from_zfast_f32(dw, h->d_weight, h->grid, h->stream);
+        }
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    cudaFree(dt);
+    cudaFree(dw);
+    if (e != cudaSuccess) return fail(h, KF_ERR_CUDA, std::string("kf_set_volume: ") + cudaGetErrorString(e));
+    return KF_OK;
+}
+
+kf_status kf_get_depth(kf_handle* h, float* depth)
+{
+    KF_HANDLE(h);
+    if (!depth) return fail(h, KF_ERR_INVALID_ARGUMENT, "null depth");
+    KF_CUDA(h, cudaMemcpyAsync(depth, h->d_depth, sizeof(float) * h->cam.H * h->cam.W, cudaMemcpyDeviceToHost,
+                               h->stream));
+    KF_CUDA(h, cudaStreamSynchronize(h->stream));
+    return KF_OK;
+}
+
+kf_status kf_get_icp_stats(kf_handle* h, int32_t* ncorr, int32_t* chol_ok, float* poses, int n)
+{
+    KF_HANDLE(h);
+    if (n < 0) return fail(h, KF_ERR_INVALID_ARGUMENT, "negative count");
+    KF_TRY(read_state(h));
+    const int m = n < kMaxIcpIters ? n : kMaxIcpIters;
+    for (int k = 0; k < m; ++k) {
+        if (ncorr) ncorr[k] = h->h_state->ncorr[k];
+        if (chol_ok) chol_ok[k] = h->h_state->chol_ok[k];
+        if (poses) std::memcpy(poses + 16 * k, h->h_state->Tlog[k], sizeof(float) * 16);
+    }
+    return KF_OK;
+}
+
+kf_status kf_set_depth_f32(kf_handle* h, const float* depth)
+{
+    KF_HANDLE(h);
+    if (!depth) return fail(h, KF_ERR_INVALID_ARGUMENT, "null depth");
+    KF_CUDA(h, cudaMemcpyAsync(h->d_depth, depth, sizeof(float) * h->cam.H * h->cam.W, cudaMemcpyHostToDevice,
+                               h->stream));
+    KF_CUDA(h, cudaStreamSynchronize(h->stream));
+    return KF_OK;
+}
+
+kf_status kf_set_depth_u16(kf_handle* h, const uint16_t* depth)
+{
+    KF_HANDLE(h);
+    if (!depth) return fail(h, KF_ERR_INVALID_ARGUMENT, "null depth");
+    KF_TRY(upload_raw(h, depth));
+    enq_ingest(h, h->d_raw, false, false);
+    KF_CHECK_LAUNCH(h);
+    KF_CUDA(h, cudaStreamSynchronize(h->stream));
+    return KF_OK;
+}
+
+kf_status kf_calculate_vertices_and_normals(kf_handle* h, float* vx, float* vy, float* nx, float* ny, float* nz,
+                                            uint8_t* mask)
+{
+    KF_HANDLE(h);
+    enq_ingest(h, nullptr, false, true);
+    KF_CHECK_LAUNCH(h);
+    if (!vx && !vy && !nx && !ny && !nz && !mask) {
+        KF_CUDA(h, cudaStreamSynchronize(h->stream));
+        return KF_OK;
+    }
+    const size_t HW = (size_t)h->cam.H * h->cam.W;
+    std::vector<float4> v(HW), n(HW);
+    KF_CUDA(h, cudaMemcpyAsync(v.data(), h->d_vmap, sizeof(float4) * HW, cudaMemcpyDeviceToHost, h->stream));
+    KF_CUDA(h, cudaMemcpyAsync(n.data(), h->d_nmap, sizeof(float4) * HW, cudaMemcpyDeviceToHost, h->stream));
+    KF_CUDA(h, cudaStreamSynchronize(h->stream));
+    for (size_t i = 0; i < HW; ++i) {
+        if (vx) vx[i] = v[i].x;
+        if (vy) vy[i] = v[i].y;
+        if (nx) nx[i] = n[i].x;
+        if (ny) ny[i] = n[i].y;
+        if (nz) nz[i] = n[i].z;
+        if (mask) mask[i] = v[i].w != 0.f ? 1 : 0;
+    }
+    return KF_OK;
+}
+
+kf_status kf_bilateral_filtering(kf_handle* h)
+{
+    KF_HANDLE(h);
+    if (!h->cfg.bilateral) {
+        // the spatial kernel is uploaded on first use for handles created without it
+        h->cfg.bilateral = 1;
+        kf_status s = upload_spatial(h);
+        h->cfg.bilateral = 0;
+        if (s != KF_OK) return s;
+    }
+    enq_bilateral(h);
+    KF_CHECK_LAUNCH(h);
+    KF_CUDA(h, cudaStreamSynchronize(h->stream));
+    return KF_OK;
+}
+
+kf_status kf_estimate_sensor_pose(kf_handle* h)
+{
+    KF_HANDLE(h);
+    // re-derive the frame-start ICP state from the current pose; the vertex map is
+    // left as the last kf_calculate_vertices_and_normals produced it
+    launch_vertex(nullptr, h->d_depth, h->d_vmap, h->d_nmap, h->cam, h->cfg.min_depth, h->cfg.max_depth,
+                  h->d_state, true, false, h->stream);
+    enq_icp(h);
+    KF_CHECK_LAUNCH(h);
+    KF_CUDA(h, cudaStreamSynchronize(h->stream));
+    return KF_OK;
+}
+
+kf_status kf_projective_tsdf(kf_handle* h, int first_tsdf_construct)
+{
+    KF_HANDLE(h);
+    enq_integrate(h, first_tsdf_construct != 0);
+    KF_CHECK_LAUNCH(h);
+    KF_CUDA(h, cudaStreamSynchronize(h->stream));
+    return KF_OK;
+}
+
+kf_status kf_ray_casting(kf_handle* h, int32_t* hit)
+{
+    KF_HANDLE(h);
+    enq_raycast(h, h->d_hit);
+    KF_CHECK_LAUNCH(h);
+    if (hit)
+        KF_CUDA(h, cudaMemcpyAsync(hit, h->d_hit, sizeof(int32_t) * h->cam.H * h->cam.W, cudaMemcpyDeviceToHost,
+                                   h->stream));
+    KF_CUDA(h, cudaStreamSynchronize(h->stream));
+    return KF_OK;
+}
+
+kf_status kf_icp_associate(kf_handle* h, const float F[16], const float T[16], int32_t* pair, float* sums27,
+                           int32_t* ncorr)
+{
+    KF_HANDLE(h);
+    if (!F || !T) return fail(h, KF_ERR_INVALID_ARGUMENT, "null transform");
+    float mats[32];
+    std::memcpy(mats, F, sizeof(float) * 16);
+    std::memcpy(mats + 16, T, sizeof(float) * 16);
+    KF_CUDA(h, cudaMemcpyAsync(h->d_mats, mats, sizeof(mats), cudaMemcpyHostToDevice, h->stream));
+    launch_icp_associate(h->d_vmap, h->d_nmap, h->d_pv, h->d_pn, h->cam, h->icp, h->d_mats, h->d_mats + 16,
+                         h->d_state, h->d_partials, h->d_mats + 32, pair ? h->d_pair : nullptr, h->stream);
+    KF_CHECK_LAUNCH(h);
+    float sums[kIcpVals];
+    KF_CUDA(h, cudaMemcpyAsync(sums, h->d_mats + 32, sizeof(sums), cudaMemcpyDeviceToHost, h->stream));
+    if (pair)
+        KF_CUDA(h, cudaMemcpyAsync(pair, h->d_pair, sizeof(int32_t) * h->cam.H * h->cam.W, cudaMemcpyDeviceToHost,
+                                   h->stream));
+    KF_CUDA(h, cudaStreamSynchronize(h->stream));
+    if (sums27) std::memcpy(sums27, sums, sizeof(float) * 27);
+    if (ncorr) *ncorr = (int32_t)sums[kIcpVals - 1];
+    return KF_OK;
+}
+
+kf_status kf_get_flip_threshold(kf_handle* h, float* c_flip)
+{
+    KF_HANDLE(h);
+    if (!c_flip) return fail(h, KF_ERR_INVALID_ARGUMENT, "null output");
+    KF_TRY(read_state(h));
+    *c_flip = h->h_state->c_flip;
+    return KF_OK;
+}
+
+kf_status kf_enable_stage_timing(kf_handle* h, int enable)
+{
+    KF_HANDLE(h);
+    KF_CUDA(h, cudaStreamSynchronize(h->stream));
+    if ((enable != 0) != h->timing) {
+        h->timing = enable != 0;
+        destroy_graphs(h);
+    }
+    return KF_OK;
+}
+
+kf_status kf_get_stage_times(kf_handle* h, float ms[5])
+{
+    KF_HANDLE(h);
+    if (!ms) return fail(h, KF_ERR_INVALID_ARGUMENT, "null output");
+    KF_TRY(kf_synchronize(h));
+    std::memcpy(ms, h->stage_ms, sizeof(float) * 5);
+    return KF_OK;
+}
+
+kf_status kf_kernels_per_frame(kf_handle* h, int* n)
+{
+    if (!h || !n) return KF_ERR_INVALID_ARGUMENT;
+    // vertex, [bilateral], ICP iterations, integration prep, integration, ray cast
+    *n = 1 + (h->cfg.bilateral ? 1 : 0) + h->cfg.icp_iterations[0] + 3;
+    return KF_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,268 @@
+// Depth ingest, vertex/normal map, bilateral filter and small utility kernels.
+#include "kf_kernels.h"
+
+namespace kf {
+
+namespace {
+
+__global__ void fill_nan_kernel(float* p, size_t n)
+{
+    const float v = qnan();
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        p[i] = v;
+}
+
+__global__ void fill_nan_half2_kernel(__half2* p, size_t n)
+{
+    const __half h = __ushort_as_half(0x7e00);
+    const __half2 v = __halves2half2(h, h);
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        p[i] = v;
+}
+
+__device__ __forceinline__ float ingest(uint16_t raw, float dmin, float dmax)
+{
+    // LoadDepthData's convertTo + GetRangeDepth's inclusive cv::inRange mask
+    // (system_utility.cpp:58-68, 77-85)
+    const float d = (float)raw;
+    return (d >= dmin && d <= dmax) ? d : 0.f;
+}
+
+// raw_vertices.cu:3-51.  One thread per pixel; the mask is kept in vmap.w.
+template <bool RAW>
+__global__ void __launch_bounds__(256) vertex_kernel(const uint16_t* __restrict__ raw, float* __restrict__ depth,
+                                                     float4* __restrict__ vmap, float4* __restrict__ nmap, Camera cam,
+                                                     float dmin, float dmax, State* st, int init_icp, int normals)
+{
+    const int H = cam.H, W = cam.W;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (init_icp && i == 0) {
+        // frame start of Estimate_Sensor_Pose (sensor_pose_estimation.cu:255-259, 343)
+        inv4(st->T, st->Tprev_inv);
+        mat4(st->Tprev_inv, st->T, st->F);
+        for (int k = 0; k < 16; ++k) st->Td[k] = (double)st->T[k];
+        st->iter = 0;
+    }
+    if (i >= H * W) return;
+    const int row = i / W, col = i % W;
+    float d;
+    if (RAW) {
+        d = ingest(raw[i], dmin, dmax);
+        depth[i] = d;
+    } else {
+        d = depth[i];
+    }
+    if (!normals) return;
+    float4 v = make_float4(0.f, 0.f, d, 0.f);
+    float4 n = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (d != 0 && row != H - 1 && col != W - 1) {
+        v.w = 1.f;
+        const int down = (row + 1) * W + col;
+        const int right = row * W + col + 1;
+        const float dd = RAW ? ingest(raw[down], dmin, dmax) : depth[down];
+        const float dr = RAW ? ingest(raw[right], dmin, dmax) : depth[right];
+        if (down > 0 && right > 0 && dd != 0 && dr != 0) {
+            const float* Ki = cam.Ki;
+            const float X = (float)(col + 1), Y = (float)(row + 1);
+            const float px = d * (Ki[0] * X + Ki[1] * Y + Ki[2]);
+            const float py = d * (Ki[3] * X + Ki[4] * Y + Ki[5]);
+            const float dx = dd * (Ki[0] * X + Ki[1] * (float)(row + 2) + Ki[2]);
+            const float rx = dr * (Ki[0] * (float)(col + 2) + Ki[1] * Y + Ki[2]);
+            const float dy = dd * (Ki[3] * X + Ki[4] * (float)(row + 2) + Ki[5]);
+            const float ry = dr * (Ki[3] * (float)(col + 2) + Ki[4] * Y + Ki[5]);
+            // (v_down - v) x (v_right - v)
+            const float n0 = (dy - py) * (dr - d) - (dd - d) * (ry - py);
+            const float n1 = (dd - d) * (rx - px) - (dx - px) * (dr - d);
+            const float n2 = (dx - px) * (ry - py) - (dy - py) * (rx - px);
+            const float len = sqrtf(n0 * n0 + n1 * n1 + n2 * n2);
+            v.x = px;
+            v.y = py;
+            n = make_float4(n0 / len, n1 / len, n2 / len, 0.f);
+        }
+    }
+    vmap[i] = v;
+    nmap[i] = n;
+}
+
+constexpr int kBilTx = 32, kBilTy = 8, kBilMaxR = 7;
+
+// bilateral_filtering.cu:3-47 with the interior bound tightened to y <= H-1-r,
+// x <= W-1-r so the 7x7 window never leaves the image (the reference's `<= H - r`
+// reads one row/column past it); pixels outside the interior are 0, as the reference's
+// zero-initialised output buffer leaves them.
+__global__ void __launch_bounds__(kBilTx* kBilTy) bilateral_kernel(const float* __restrict__ depth,
+                                                                    float* __restrict__ out,
+                                                                    const float* __restrict__ spatial, int r,
+                                                                    float sigma_r, int H, int W)
+{
+    __shared__ float tile[(kBilTy + 2 * kBilMaxR) * (kBilTx + 2 * kBilMaxR)];
+    __shared__ float sw[(2 * kBilMaxR + 1) * (2 * kBilMaxR + 1)];
+    const int kl = 2 * r + 1;
+    const int tw = kBilTx + 2 * r, th = kBilTy + 2 * r;
+    const int x0 = blockIdx.x * kBilTx - r, y0 = blockIdx.y * kBilTy - r;
+    const int tid = threadIdx.y * kBilTx + threadIdx.x;
+    for (int k = tid; k < kl * kl; k += kBilTx * kBilTy) sw[k] = spatial[k];
+    for (int k = tid; k < tw * th; k += kBilTx * kBilTy) {
+        const int gx = x0 + k % tw, gy = y0 + k / tw;
+        tile[k] = (gx >= 0 && gx < W && gy >= 0 && gy < H) ? depth[gy * W + gx] : 0.f;
+    }
+    __syncthreads();
+    const int x = blockIdx.x * kBilTx + threadIdx.x, y = blockIdx.y * kBilTy + threadIdx.y;
+    if (x >= W || y >= H) return;
+    float res = 0.f;
+    if (y >= r && y <= H - 1 - r && x >= r && x <= W - 1 - r) {
+        const float c = tile[(threadIdx.y + r) * tw + threadIdx.x + r];
+        const float denom = 2 * sigma_r * sigma_r;
+        float sum = 0.f;
+        for (int dy = 0; dy < kl; ++dy)
+            for (int dx = 0; dx < kl; ++dx) {
+                float t = tile[(threadIdx.y + dy) * tw + threadIdx.x + dx] - c;
+                t = expf(-(t * t) / denom);
+                sum = sum + (sw[dy * kl + dx] * t + 0.000000001f);
+            }
+        float acc = 0.f;
+        for (int dy = 0; dy < kl; ++dy)
+            for (int dx = 0; dx < kl; ++dx) {
+                const float v = tile[(threadIdx.y + dy) * tw + threadIdx.x + dx];
+                float t = v - c;
+                t = expf(-(t * t) / denom);
+                const float wt = sw[dy * kl + dx] * t + 0.000000001f;
+                acc = acc + (wt / sum) * v;
+            }
+        res = acc;
+    }
+    out[y * W + x] = res;
+}
+
+// flip iff acos(c) * (180/pi) > 90 (voxel_traversal.cu:361-364, double acos).  acos is
+// monotone, so over floats the predicate is "c below a threshold"; find the threshold
+// with the device's own acos by bisection over the float order in [-1e-3, 1e-3].
+__device__ bool flips(float c)
+{
+    const double angle = acos((double)c) * (180.0f / 3.141592654f);
+    return angle > 90;
+}
+
+__device__ __forceinline__ int float_key(float f)
+{
+    const int b = __float_as_int(f);
+    return b >= 0 ? b : -(b & 0x7fffffff);
+}
+
+__device__ __forceinline__ float key_float(int k) { return k >= 0 ? __int_as_float(k) : -__int_as_float(-k); }
+
+__global__ void calibrate_kernel(State* st)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    int lo = float_key(-1e-3f), hi = float_key(1e-3f);  // flips(lo) true, flips(hi) false
+    for (int it = 0; it < 64 && hi - lo > 1; ++it) {
+        const int mid = lo + (hi - lo) / 2;
+        if (flips(key_float(mid)))
+            lo = mid;
+        else
+            hi = mid;
+    }
+    st->c_flip = key_float(hi);
+}
+
+// x-fastest (device) <-> z-fastest (reference) volume order
+__global__ void to_zfast_kernel(const float* __restrict__ src, float* __restrict__ dst, Grid g)
+{
+    const size_t n = (size_t)g.dx * g.dy * g.dz;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const size_t x = i % g.dx, y = (i / g.dx) % g.dy, z = i / ((size_t)g.dx * g.dy);
+        dst[(x * g.dy + y) * g.dz + z] = src[i];
+    }
+}
+
+__global__ void from_zfast_kernel(const float* __restrict__ src, float* __restrict__ dst, Grid g)
+{
+    const size_t n = (size_t)g.dx * g.dy * g.dz;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const size_t x = i % g.dx, y = (i / g.dx) % g.dy, z = i / ((size_t)g.dx * g.dy);
+        dst[i] = src[(x * g.dy + y) * g.dz + z];
+    }
+}
+
+__global__ void half2_to_zfast_kernel(const __half2* __restrict__ src, float* __restrict__ tsdf,
+                                      float* __restrict__ weight, Grid g)
+{
+    const size_t n = (size_t)g.dx * g.dy * g.dz;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const size_t x = i % g.dx, y = (i / g.dx) % g.dy, z = i / ((size_t)g.dx * g.dy);
+        const float2 v = __half22float2(src[i]);
+        const size_t j = (x * g.dy + y) * g.dz + z;
+        tsdf[j] = v.x;
+        weight[j] = v.y;
+    }
+}
+
+__global__ void zfast_to_half2_kernel(const float* __restrict__ tsdf, const float* __restrict__ weight,
+                                      __half2* __restrict__ dst, Grid g)
+{
+    const size_t n = (size_t)g.dx * g.dy * g.dz;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const size_t x = i % g.dx, y = (i / g.dx) % g.dy, z = i / ((size_t)g.dx * g.dy);
+        const size_t j = (x * g.dy + y) * g.dz + z;
+        dst[i] = __floats2half2_rn(tsdf[j], weight[j]);
+    }
+}
+
+int grid_for(size_t n, int block)
+{
+    const size_t b = (n + block - 1) / block;
+    return (int)(b < 152 * 32 ? (b == 0 ? 1 : b) : 152 * 32);
+}
+
+}  // namespace
+
+void launch_fill_nan(float* p, size_t n, cudaStream_t s) { fill_nan_kernel<<<grid_for(n, 256), 256, 0, s>>>(p, n); }
+
+void launch_fill_nan_half2(__half2* p, size_t n, cudaStream_t s)
+{
+    fill_nan_half2_kernel<<<grid_for(n, 256), 256, 0, s>>>(p, n);
+}
+
+void launch_vertex(const uint16_t* raw, float* depth, float4* vmap, float4* nmap, const Camera& cam, float dmin,
+                   float dmax, State* st, bool init_icp, bool compute_normals, cudaStream_t s)
+{
+    const int n = cam.H * cam.W;
+    const int blocks = (n + 255) / 256;
+    if (raw)
+        vertex_kernel<true><<<blocks, 256, 0, s>>>(raw, depth, vmap, nmap, cam, dmin, dmax, st, init_icp ? 1 : 0,
+                                                   compute_normals ? 1 : 0);
+    else
+        vertex_kernel<false><<<blocks, 256, 0, s>>>(raw, depth, vmap, nmap, cam, dmin, dmax, st, init_icp ? 1 : 0,
+                                                    compute_normals ? 1 : 0);
+}
+
+void launch_bilateral(const float* depth, float* out, const float* spatial, int r, float sigma_r, int H, int W,
+                      cudaStream_t s)
+{
+    dim3 block(kBilTx, kBilTy), grid((W + kBilTx - 1) / kBilTx, (H + kBilTy - 1) / kBilTy);
+    bilateral_kernel<<<grid, block, 0, s>>>(depth, out, spatial, r, sigma_r, H, W);
+}
+
+void launch_calibrate(State* st, cudaStream_t s) { calibrate_kernel<<<1, 32, 0, s>>>(st); }
+
+void launch_to_zfast_f32(const float* src, float* dst, const Grid& g, cudaStream_t s)
+{
+    to_zfast_kernel<<<152 * 16, 256, 0, s>>>(src, dst, g);
+}
+
+void launch_from_zfast_f32(const float* src, float* dst, const Grid& g, cudaStream_t s)
+{
+    from_zfast_kernel<<<152 * 16, 256, 0, s>>>(src, dst, g);
+}
+
+void launch_half2_to_zfast(const __half2* src, float* tsdf, float* weight, const Grid& g, cudaStream_t s)
+{
+    half2_to_zfast_kernel<<<152 * 16, 256, 0, s>>>(src, tsdf, weight, g);
+}
+
+void launch_zfast_to_half2(const float* tsdf, const float* weight, __half2* dst, const Grid& g, cudaStream_t s)
+{
+    zfast_to_half2_kernel<<<152 * 16, 256, 0, s>>>(tsdf, weight, dst, g);
+}
+
+}  // namespace kf

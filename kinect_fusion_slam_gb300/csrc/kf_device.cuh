@@ -1,0 +1,83 @@
+// Device-side types and helpers shared by the kinfu_gb300 kernels.
+#pragma once
+
+#include <cstdint>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include "kf_math.cuh"
+
+namespace kf {
+
+constexpr int kMaxIcpIters = 64;
+// per-block ICP partial: 6 sums of a*b, 21 of the upper triangle of a a^T, count
+constexpr int kIcpVals = 28;
+
+// The voxel grid.  Device layout is x-fastest: lin = (z*dy + y)*dx + x; the
+// reference's z-fastest index is (x*dy + y)*dz + z (kinfu_pipeline.cpp:53-55).
+struct Grid {
+    int dx, dy, dz;
+    int sx, sy, sz;  // integer voxel coordinate of voxel (0,0,0)
+    float vd;        // voxel size, mm
+    float trunc, sdf_min, sdf_max;
+};
+
+struct Camera {
+    int H, W;
+    float K[9], Ki[9];
+};
+
+struct IcpParams {
+    float dist;       // mm
+    float angle_deg;  // degrees
+    int fail_mode;    // 0 reference (raw b), 1 identity
+    int precise;      // compensated sums + FP64 solve
+};
+
+// Per-handle device state, updated by the kernels so that a whole frame runs without
+// host round trips.
+struct State {
+    float T[16];          // extrinsic_matrix: camera-to-world pose
+    float Tprev_inv[16];  // inverse of the pose at the start of the frame's ICP
+    float F[16];          // Tprev_inv * T, the frame-to-frame transform of the iteration
+    float Tinv[16];       // inverse of the pose used by integration
+    float axis[3];        // "in front of the camera" direction (projective_tsdf.cu:57-71)
+    float c_flip;         // ray-cast normal flip threshold (voxel_traversal.cu:361-369)
+    double Td[16];        // FP64 pose (precise solve mode)
+    unsigned ticket;      // last-block election counter of the ICP reduction
+    int iter;             // ICP iterations done in the current frame
+    int32_t ncorr[kMaxIcpIters];
+    int32_t chol_ok[kMaxIcpIters];
+    float Tlog[kMaxIcpIters][16];  // pose after each iteration
+    float sums[kIcpVals];  // sums of the most recent ICP iteration
+};
+
+// voxel-centre coordinate, kinfu_pipeline.cpp:53-55: x * voxel_distance + voxel_distance / 2
+__device__ __forceinline__ float centre(int index, int start, float vd)
+{
+    return (float)(index + start) * vd + vd / 2.f;
+}
+
+// rows 0..2 of a 4x4 row-major transform applied to a point, ((m0 x + m1 y) + m2 z) + m3
+__device__ __forceinline__ float3 xform(const float* m, float3 p)
+{
+    return make_float3(m[0] * p.x + m[1] * p.y + m[2] * p.z + m[3], m[4] * p.x + m[5] * p.y + m[6] * p.z + m[7],
+                       m[8] * p.x + m[9] * p.y + m[10] * p.z + m[11]);
+}
+
+__device__ __forceinline__ float3 mul3(const float* m, float3 p)
+{
+    return make_float3(m[0] * p.x + m[1] * p.y + m[2] * p.z, m[3] * p.x + m[4] * p.y + m[5] * p.z,
+                       m[6] * p.x + m[7] * p.y + m[8] * p.z);
+}
+
+// Get_Normalized, cuda_functions.cuh:1-10
+__device__ __forceinline__ float3 normalized(float3 v)
+{
+    const float r = 1 / sqrtf(v.x * v.x + v.y * v.y + v.z * v.z);
+    return make_float3(v.x * r, v.y * r, v.z * r);
+}
+
+__device__ __forceinline__ float qnan() { return __int_as_float(0x7fc00000); }
+
+}  // namespace kf

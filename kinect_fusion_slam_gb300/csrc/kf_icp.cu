@@ -1,0 +1,319 @@
+// Projective point-to-plane ICP: association, one-pass reduction of the 6x6 normal
+// equations and the on-device solve (sensor_pose_estimation.cu:7-136, 247-436).
+//
+// One launch per iteration.  Every thread associates its pixels and accumulates the
+// 27 distinct sums of the reference's 42 planes (6 of a*b, the upper triangle of
+// a a^T; the reference's A is exactly symmetric because a_r*a_s == a_s*a_r and both
+// planes are summed in the same order) plus a correspondence count in registers; the
+// block reduces them with warp shuffles and shared memory and writes one partial; the
+// last block to finish (ticket counter) reduces the partials in a fixed order, solves
+// the system like cv::Cholesky, forms the small-angle increment and updates the pose
+// in device memory.  The reduction order differs from the reference's 64-wide tree +
+// serial host sum, so the sums agree to float rounding, not bit for bit.
+#include <cstddef>
+
+#include "kf_kernels.h"
+
+namespace kf {
+
+namespace {
+
+constexpr int kIcpBlock = 256;
+constexpr int kIcpMaxBlocks = 152 * 4;
+
+struct TwoSum {
+    float hi, lo;
+};
+
+// Knuth's two-sum: hi + lo == a + b exactly (no FMA contraction in this file)
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e)
+{
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
+template <bool PRECISE>
+struct Acc {
+    float hi[kIcpVals];
+    float lo[PRECISE ? kIcpVals : 1];
+
+    __device__ __forceinline__ void zero()
+    {
+#pragma unroll
+        for (int k = 0; k < kIcpVals; ++k) hi[k] = 0.f;
+        if (PRECISE) {
+#pragma unroll
+            for (int k = 0; k < kIcpVals; ++k) lo[PRECISE ? k : 0] = 0.f;
+        }
+    }
+    __device__ __forceinline__ void add(int k, float v)
+    {
+        if (PRECISE) {
+            float s, e;
+            two_sum(hi[k], v, s, e);
+            hi[k] = s;
+            lo[PRECISE ? k : 0] += e;
+        } else {
+            hi[k] += v;
+        }
+    }
+    __device__ __forceinline__ void add_pair(int k, float h, float l)
+    {
+        if (PRECISE) {
+            float s, e;
+            two_sum(hi[k], h, s, e);
+            hi[k] = s;
+            lo[PRECISE ? k : 0] += e + l;
+        } else {
+            hi[k] += h;
+        }
+    }
+};
+
+__device__ __forceinline__ bool associate(int i, const float4* __restrict__ vmap, const float4* __restrict__ nmap,
+                                          const float4* __restrict__ pv, const float4* __restrict__ pn,
+                                          const Camera& cam, const float* F, const float* T, float dist_th,
+                                          float ang_th, float (&a)[6], float& b, int& j)
+{
+    const float4 v = vmap[i];
+    // sensor_pose_estimation.cu:20 (vmap.w holds the vertex mask)
+    if (!(v.z != 0 && v.w != 0)) return false;
+    const float3 p3 = make_float3(v.x, v.y, v.z);
+    const float3 c = xform(F, p3);
+    // the reference projects through K (its kernel argument named dev_inv_cam_intrinsic
+    // receives dev_cam_intrinsic at :353)
+    const float3 p = mul3(cam.K, c);
+    const int u = (int)roundf(p.x / p.z);
+    const int vv = (int)roundf(p.y / p.z);
+    if (!(u > 0 && u <= cam.W && vv > 0 && vv <= cam.H)) return false;
+    const float3 g = xform(T, p3);
+    j = (vv - 1) * cam.W + (u - 1);
+    const float4 q = pv[j];
+    const float4 m = pn[j];
+    const float3 dd = make_float3(g.x - q.x, g.y - q.y, g.z - q.z);
+    const float dist = sqrtf(dd.x * dd.x + dd.y * dd.y + dd.z * dd.z);
+    if (!(dist <= dist_th && dist >= 0.0f)) return false;
+    const float4 n = nmap[i];
+    const float3 un = normalized(make_float3(T[0] * n.x + T[1] * n.y + T[2] * n.z, T[4] * n.x + T[5] * n.y + T[6] * n.z,
+                                             T[8] * n.x + T[9] * n.y + T[10] * n.z));
+    const float3 va = normalized(make_float3(m.x, m.y, m.z));
+    const float ct = un.x * va.x + un.y * va.y + un.z * va.z;
+    const float angle = acosf(ct) * (180.0f / 3.141592654f);
+    if (!(angle <= ang_th && angle >= 0.0f)) return false;
+    a[0] = g.z * m.y + (-g.y * m.z);
+    a[1] = -g.z * m.x + (g.x * m.z);
+    a[2] = g.y * m.x + (-g.x * m.y);
+    a[3] = m.x;
+    a[4] = m.y;
+    a[5] = m.z;
+    b = m.x * (q.x - g.x) + m.y * (q.y - g.y) + m.z * (q.z - g.z);
+    return true;
+}
+
+// Deterministic block reduction: butterfly shuffles within each warp, then warp
+// partials summed in warp order by threads 0..kIcpVals-1.  Result in out[] (shared).
+template <bool PRECISE>
+__device__ __forceinline__ void block_reduce(Acc<PRECISE>& acc, float* sh_hi, float* sh_lo, float* out_hi,
+                                             float* out_lo)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    constexpr int nw = kIcpBlock / 32;
+#pragma unroll
+    for (int k = 0; k < kIcpVals; ++k) {
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            const float h = __shfl_xor_sync(0xffffffffu, acc.hi[k], off);
+            const float l = PRECISE ? __shfl_xor_sync(0xffffffffu, acc.lo[PRECISE ? k : 0], off) : 0.f;
+            acc.add_pair(k, h, l);
+        }
+    }
+    if (lane == 0) {
+#pragma unroll
+        for (int k = 0; k < kIcpVals; ++k) {
+            sh_hi[warp * kIcpVals + k] = acc.hi[k];
+            if (PRECISE) sh_lo[warp * kIcpVals + k] = acc.lo[PRECISE ? k : 0];
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < kIcpVals) {
+        const int k = threadIdx.x;
+        float h = sh_hi[k], l = PRECISE ? sh_lo[k] : 0.f;
+        for (int w = 1; w < nw; ++w) {
+            if (PRECISE) {
+                float s, e;
+                two_sum(h, sh_hi[w * kIcpVals + k], s, e);
+                h = s;
+                l += e + sh_lo[w * kIcpVals + k];
+            } else {
+                h += sh_hi[w * kIcpVals + k];
+            }
+        }
+        out_hi[k] = h;
+        if (PRECISE) out_lo[k] = l;
+    }
+    __syncthreads();
+}
+
+__device__ __forceinline__ int tri(int r, int s) { return 6 + r * 6 - r * (r - 1) / 2 + (s - r); }
+
+// MODE 0: one ICP iteration (F, T from the state; the last block updates the pose).
+// MODE 1: association + reduction at the given F, T; the last block writes the sums.
+template <bool PRECISE, int MODE>
+__global__ void __launch_bounds__(kIcpBlock) icp_kernel(const float4* __restrict__ vmap, const float4* __restrict__ nmap,
+                                                      const float4* __restrict__ pv, const float4* __restrict__ pn,
+                                                      Camera cam, IcpParams prm, State* st, const float* Fsrc,
+                                                      const float* Tsrc, float* partials, float* sums_out,
+                                                      int32_t* pair)
+{
+    __shared__ float sF[16], sT[16];
+    __shared__ float sh_hi[(kIcpBlock / 32) * kIcpVals];
+    __shared__ float sh_lo[PRECISE ? (kIcpBlock / 32) * kIcpVals : 1];
+    __shared__ float red_hi[kIcpVals], red_lo[kIcpVals];
+    __shared__ int is_last;
+    if (threadIdx.x < 16) {
+        sF[threadIdx.x] = Fsrc[threadIdx.x];
+        sT[threadIdx.x] = Tsrc[threadIdx.x];
+    }
+    __syncthreads();
+
+    Acc<PRECISE> acc;
+    acc.zero();
+    const int n = cam.H * cam.W;
+    for (int i = blockIdx.x * kIcpBlock + threadIdx.x; i < n; i += gridDim.x * kIcpBlock) {
+        float a[6], b;
+        int j = -1;
+        const bool ok = associate(i, vmap, nmap, pv, pn, cam, sF, sT, prm.dist, prm.angle_deg, a, b, j);
+        if (MODE == 1 && pair) pair[i] = ok ? j : -1;
+        if (!ok) continue;
+#pragma unroll
+        for (int r = 0; r < 6; ++r) acc.add(r, a[r] * b);
+#pragma unroll
+        for (int r = 0; r < 6; ++r)
+#pragma unroll
+            for (int s = r; s < 6; ++s) acc.add(tri(r, s), a[r] * a[s]);
+        acc.add(kIcpVals - 1, 1.f);
+    }
+    block_reduce<PRECISE>(acc, sh_hi, sh_lo, red_hi, red_lo);
+
+    // publish this block's partial; the last block to arrive finishes the reduction
+    float* part_hi = partials;
+    float* part_lo = partials + (size_t)gridDim.x * kIcpVals;
+    if (threadIdx.x < kIcpVals) {
+        part_hi[blockIdx.x * kIcpVals + threadIdx.x] = red_hi[threadIdx.x];
+        if (PRECISE) part_lo[blockIdx.x * kIcpVals + threadIdx.x] = red_lo[threadIdx.x];
+        __threadfence();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) is_last = (atomicAdd(&st->ticket, 1u) == gridDim.x - 1);
+    __syncthreads();
+    if (!is_last) return;
+    __threadfence();
+
+    acc.zero();
+    for (int bidx = threadIdx.x; bidx < (int)gridDim.x; bidx += kIcpBlock) {
+#pragma unroll
+        for (int k = 0; k < kIcpVals; ++k)
+            acc.add_pair(k, __ldcg(part_hi + bidx * kIcpVals + k), PRECISE ? __ldcg(part_lo + bidx * kIcpVals + k) : 0.f);
+    }
+    block_reduce<PRECISE>(acc, sh_hi, sh_lo, red_hi, red_lo);
+    if (threadIdx.x != 0) return;
+    st->ticket = 0u;
+
+    if (MODE == 1) {
+        for (int k = 0; k < kIcpVals; ++k) sums_out[k] = PRECISE ? red_hi[k] + red_lo[k] : red_hi[k];
+        return;
+    }
+
+    const int it = st->iter;
+    for (int k = 0; k < kIcpVals; ++k) st->sums[k] = PRECISE ? red_hi[k] + red_lo[k] : red_hi[k];
+    bool ok;
+    if (!PRECISE) {
+        float A[36], x[6];
+        for (int r = 0; r < 6; ++r)
+            for (int s = r; s < 6; ++s) A[r * 6 + s] = A[s * 6 + r] = red_hi[tri(r, s)];
+        for (int r = 0; r < 6; ++r) x[r] = red_hi[r];
+        // cv::Cholesky; on failure the reference keeps b untouched and applies it
+        ok = chol6(A, x);
+        if (!ok && prm.fail_mode == 1)
+            for (int r = 0; r < 6; ++r) x[r] = 0.f;
+        float inc[16];
+        increment(x, inc);
+        mat4(inc, st->T, st->T);
+    } else {
+        double A[36], x[6];
+        for (int r = 0; r < 6; ++r)
+            for (int s = r; s < 6; ++s)
+                A[r * 6 + s] = A[s * 6 + r] = (double)red_hi[tri(r, s)] + (double)red_lo[tri(r, s)];
+        for (int r = 0; r < 6; ++r) x[r] = (double)red_hi[r] + (double)red_lo[r];
+        ok = chol6_f64(A, x);
+        if (!ok) {
+            if (prm.fail_mode == 1)
+                for (int r = 0; r < 6; ++r) x[r] = 0.0;
+            else
+                for (int r = 0; r < 6; ++r) x[r] = (double)red_hi[r] + (double)red_lo[r];
+        }
+        // SE(3) composition in FP64: the same small-angle increment, applied to the FP64 pose
+        const double inc[16] = {1.0, x[2], -x[1], x[3], -x[2], 1.0, x[0], x[4],
+                                x[1], -x[0], 1.0, x[5], 0.0, 0.0, 0.0, 1.0};
+        double R[16];
+        for (int r = 0; r < 4; ++r)
+            for (int c = 0; c < 4; ++c) {
+                double s = 0.0;
+                for (int k = 0; k < 4; ++k) s += inc[r * 4 + k] * st->Td[k * 4 + c];
+                R[r * 4 + c] = s;
+            }
+        for (int k = 0; k < 16; ++k) {
+            st->Td[k] = R[k];
+            st->T[k] = (float)R[k];
+        }
+    }
+    mat4(st->Tprev_inv, st->T, st->F);
+    if (it < kMaxIcpIters) {
+        st->ncorr[it] = (int32_t)(red_hi[kIcpVals - 1] + (PRECISE ? red_lo[kIcpVals - 1] : 0.f));
+        st->chol_ok[it] = ok ? 1 : 0;
+        for (int k = 0; k < 16; ++k) st->Tlog[it][k] = st->T[k];
+    }
+    st->iter = it + 1;
+}
+
+// device addresses of State members, computed without dereferencing on the host
+const float* state_F(State* st) { return reinterpret_cast<const float*>(reinterpret_cast<char*>(st) + offsetof(State, F)); }
+const float* state_T(State* st) { return reinterpret_cast<const float*>(reinterpret_cast<char*>(st) + offsetof(State, T)); }
+
+int blocks_for(int H, int W)
+{
+    const int b = (H * W + kIcpBlock - 1) / kIcpBlock;
+    return b < kIcpMaxBlocks ? (b < 1 ? 1 : b) : kIcpMaxBlocks;
+}
+
+}  // namespace
+
+int icp_grid_blocks(int H, int W) { return blocks_for(H, W); }
+
+void launch_icp_iteration(const float4* vmap, const float4* nmap, const float4* pv, const float4* pn,
+                          const Camera& cam, const IcpParams& prm, State* st, float* partials, cudaStream_t s)
+{
+    const int blocks = blocks_for(cam.H, cam.W);
+    if (prm.precise)
+        icp_kernel<true, 0><<<blocks, kIcpBlock, 0, s>>>(vmap, nmap, pv, pn, cam, prm, st, state_F(st),
+                                                         state_T(st), partials, nullptr, nullptr);
+    else
+        icp_kernel<false, 0><<<blocks, kIcpBlock, 0, s>>>(vmap, nmap, pv, pn, cam, prm, st, state_F(st),
+                                                          state_T(st), partials, nullptr, nullptr);
+}
+
+void launch_icp_associate(const float4* vmap, const float4* nmap, const float4* pv, const float4* pn,
+                          const Camera& cam, const IcpParams& prm, const float* F, const float* T, State* st,
+                          float* partials, float* sums_out, int32_t* pair, cudaStream_t s)
+{
+    const int blocks = blocks_for(cam.H, cam.W);
+    if (prm.precise)
+        icp_kernel<true, 1><<<blocks, kIcpBlock, 0, s>>>(vmap, nmap, pv, pn, cam, prm, st, F, T, partials, sums_out,
+                                                         pair);
+    else
+        icp_kernel<false, 1><<<blocks, kIcpBlock, 0, s>>>(vmap, nmap, pv, pn, cam, prm, st, F, T, partials,
+                                                          sums_out, pair);
+}
+
+}  // namespace kf

@@ -1,0 +1,62 @@
+// Launch wrappers of the kinfu_gb300 kernels (host side; called by kf_api.cu).
+#pragma once
+
+#include <cstdint>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include "kf_device.cuh"
+
+namespace kf {
+
+// fill with the reference's NaN (0x7fc00000)
+void launch_fill_nan(float* p, size_t n, cudaStream_t s);
+void launch_fill_nan_half2(__half2* p, size_t n, cudaStream_t s);
+
+// depth ingest (+ inclusive range filter when raw != nullptr) fused with the
+// vertex/normal map of raw_vertices.cu:3-51.  With init_icp, thread 0 also prepares
+// the frame's ICP state (T_prev^-1 and F) from st->T.
+void launch_vertex(const uint16_t* raw, float* depth, float4* vmap, float4* nmap, const Camera& cam, float dmin,
+                   float dmax, State* st, bool init_icp, bool compute_normals, cudaStream_t s);
+
+// 7x7 (radius r) bilateral filter of depth into out (bilateral_filtering.cu:3-47)
+void launch_bilateral(const float* depth, float* out, const float* spatial, int r, float sigma_r, int H, int W,
+                      cudaStream_t s);
+
+// One ICP iteration: association + one-pass reduction + (last block) 6x6 solve and pose
+// update.  partials must hold icp_grid_blocks() * kIcpVals floats.
+int icp_grid_blocks(int H, int W);
+void launch_icp_iteration(const float4* vmap, const float4* nmap, const float4* pv, const float4* pn,
+                          const Camera& cam, const IcpParams& prm, State* st, float* partials, cudaStream_t s);
+// Association + reduction only at the given F, T (device pointers to 16 floats each);
+// sums_out receives kIcpVals floats (27 sums + count), pair may be nullptr.
+void launch_icp_associate(const float4* vmap, const float4* nmap, const float4* pv, const float4* pn,
+                          const Camera& cam, const IcpParams& prm, const float* F, const float* T, State* st,
+                          float* partials, float* sums_out, int32_t* pair, cudaStream_t s);
+
+// per-pixel integration table + T^-1 and the in-front axis into st
+void launch_integrate_prep(const float* depth, float2* tab, const Camera& cam, State* st, cudaStream_t s);
+// projective TSDF update (projective_tsdf.cu:5-140); skip_from = first z-fastest index
+// the reference's float guard never reaches
+void launch_integrate_f32(float* tsdf, float* weight, const float2* tab, const State* st, const Grid& g,
+                          const Camera& cam, long long skip_from, bool first, cudaStream_t s);
+void launch_integrate_f16(__half2* vol, const float2* tab, const State* st, const Grid& g, const Camera& cam,
+                          long long skip_from, bool first, cudaStream_t s);
+
+// Amanatides-Woo ray cast (voxel_traversal.cu:75-424); hit may be nullptr
+void launch_raycast_f32(const float* tsdf, const float* depth, float4* pv, float4* pn, int32_t* hit,
+                        const Camera& cam, const Grid& g, const State* st, cudaStream_t s);
+void launch_raycast_f16(const __half2* vol, const float* depth, float4* pv, float4* pn, int32_t* hit,
+                        const Camera& cam, const Grid& g, const State* st, cudaStream_t s);
+
+// st->c_flip from the device's own double acos (single thread, once per handle)
+void launch_calibrate(State* st, cudaStream_t s);
+
+// volume layout conversions between the device x-fastest order and the reference's
+// z-fastest order
+void launch_to_zfast_f32(const float* src, float* dst, const Grid& g, cudaStream_t s);
+void launch_from_zfast_f32(const float* src, float* dst, const Grid& g, cudaStream_t s);
+void launch_half2_to_zfast(const __half2* src, float* tsdf, float* weight, const Grid& g, cudaStream_t s);
+void launch_zfast_to_half2(const float* tsdf, const float* weight, __half2* dst, const Grid& g, cudaStream_t s);
+
+}  // namespace kf

@@ -1,0 +1,181 @@
+// Small-matrix routines shared by host and device code of the kinfu_gb300 library.
+//
+// The reference calls OpenCV for these on the host (cv::Mat::inv at
+// projective_tsdf.cu:148-149, voxel_traversal.cu:445-446, raw_vertices.cu:59,
+// sensor_pose_estimation.cu:255-256; Mat operator* at sensor_pose_estimation.cu:343,428;
+// cv::Cholesky at :399).  Here they run on the device inside the frame's kernels so
+// that no host round trip is needed, restated from OpenCV's published algorithms:
+//   inv3  -- closed-form adjugate, double products, one rounding to float
+//   inv4  -- float LU with partial pivoting (cv::invert DECOMP_LU, hal::LU32f)
+//   mat4  -- 4x4 product accumulated in double, rounded to float (cv::gemm)
+//   chol6 -- in-place Cholesky with double accumulators and float storage of L,
+//            reciprocal diagonal, forward/back substitution (hal::Cholesky32f);
+//            returns false and leaves b untouched when a pivot is below FLT_EPSILON.
+// Every file that includes this is compiled without FMA contraction (-fmad=false on
+// the device, -ffp-contract=off on the host), so host and device give the same bits.
+#pragma once
+
+#include <cfloat>
+#include <cmath>
+
+#if defined(__CUDACC__)
+#define KF_HD __host__ __device__ __forceinline__
+#else
+#define KF_HD inline
+#endif
+
+namespace kf {
+
+KF_HD void inv3(const float* m, float* out)
+{
+    double d = m[0] * ((double)m[4] * m[8] - (double)m[5] * m[7]) - m[1] * ((double)m[3] * m[8] - (double)m[5] * m[6]) +
+               m[2] * ((double)m[3] * m[7] - (double)m[4] * m[6]);
+    if (d == 0.0) {
+        for (int i = 0; i < 9; ++i) out[i] = 0.f;
+        return;
+    }
+    d = 1.0 / d;
+    out[0] = (float)(((double)m[4] * m[8] - (double)m[5] * m[7]) * d);
+    out[1] = (float)(((double)m[2] * m[7] - (double)m[1] * m[8]) * d);
+    out[2] = (float)(((double)m[1] * m[5] - (double)m[2] * m[4]) * d);
+    out[3] = (float)(((double)m[5] * m[6] - (double)m[3] * m[8]) * d);
+    out[4] = (float)(((double)m[0] * m[8] - (double)m[2] * m[6]) * d);
+    out[5] = (float)(((double)m[2] * m[3] - (double)m[0] * m[5]) * d);
+    out[6] = (float)(((double)m[3] * m[7] - (double)m[4] * m[6]) * d);
+    out[7] = (float)(((double)m[1] * m[6] - (double)m[0] * m[7]) * d);
+    out[8] = (float)(((double)m[0] * m[4] - (double)m[1] * m[3]) * d);
+}
+
+KF_HD bool inv4(const float* src, float* out)
+{
+    float a[16], b[16];
+    for (int i = 0; i < 16; ++i) {
+        a[i] = src[i];
+        b[i] = (i % 5 == 0) ? 1.f : 0.f;
+    }
+    const float eps = FLT_EPSILON * 10;
+    for (int i = 0; i < 4; ++i) {
+        int p = i;
+        for (int j = i + 1; j < 4; ++j)
+            if (fabsf(a[j * 4 + i]) > fabsf(a[p * 4 + i])) p = j;
+        if (fabsf(a[p * 4 + i]) < eps) {
+            for (int t = 0; t < 16; ++t) out[t] = 0.f;
+            return false;
+        }
+        if (p != i) {
+            for (int j = i; j < 4; ++j) {
+                const float t = a[i * 4 + j];
+                a[i * 4 + j] = a[p * 4 + j];
+                a[p * 4 + j] = t;
+            }
+            for (int j = 0; j < 4; ++j) {
+                const float t = b[i * 4 + j];
+                b[i * 4 + j] = b[p * 4 + j];
+                b[p * 4 + j] = t;
+            }
+        }
+        const float d = -1 / a[i * 4 + i];
+        for (int j = i + 1; j < 4; ++j) {
+            const float alpha = a[j * 4 + i] * d;
+            for (int c = i + 1; c < 4; ++c) a[j * 4 + c] += alpha * a[i * 4 + c];
+            for (int c = 0; c < 4; ++c) b[j * 4 + c] += alpha * b[i * 4 + c];
+        }
+    }
+    for (int i = 3; i >= 0; --i)
+        for (int j = 0; j < 4; ++j) {
+            float s = b[i * 4 + j];
+            for (int c = i + 1; c < 4; ++c) s -= a[i * 4 + c] * b[c * 4 + j];
+            b[i * 4 + j] = s / a[i * 4 + i];
+        }
+    for (int i = 0; i < 16; ++i) out[i] = b[i];
+    return true;
+}
+
+// out = a * b (out may alias a or b)
+KF_HD void mat4(const float* a, const float* b, float* out)
+{
+    float r[16];
+    for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 4; ++j) {
+            double s = (double)a[i * 4 + 0] * b[j];
+            s += (double)a[i * 4 + 1] * b[4 + j];
+            s += (double)a[i * 4 + 2] * b[8 + j];
+            s += (double)a[i * 4 + 3] * b[12 + j];
+            r[i * 4 + j] = (float)s;
+        }
+    for (int i = 0; i < 16; ++i) out[i] = r[i];
+}
+
+// A: 6x6 row-major, lower triangle read and overwritten; b: right-hand side -> solution
+KF_HD bool chol6(float* A, float* b)
+{
+    const int m = 6;
+    double s;
+    int i, j, k;
+    for (i = 0; i < m; ++i) {
+        for (j = 0; j < i; ++j) {
+            s = A[i * m + j];
+            for (k = 0; k < j; ++k) s -= A[i * m + k] * A[j * m + k];
+            A[i * m + j] = (float)(s * A[j * m + j]);
+        }
+        s = A[i * m + i];
+        for (k = 0; k < j; ++k) {
+            const double t = A[i * m + k];
+            s -= t * t;
+        }
+        if (s < FLT_EPSILON) return false;
+        A[i * m + i] = (float)(1. / sqrt(s));
+    }
+    for (i = 0; i < m; ++i) {
+        s = b[i];
+        for (k = 0; k < i; ++k) s -= A[i * m + k] * b[k];
+        b[i] = (float)(s * A[i * m + i]);
+    }
+    for (i = m - 1; i >= 0; --i) {
+        s = b[i];
+        for (k = m - 1; k > i; --k) s -= A[k * m + i] * b[k];
+        b[i] = (float)(s * A[i * m + i]);
+    }
+    return true;
+}
+
+// FP64 Cholesky solve of A x = b (precise solve mode); false when not positive definite
+KF_HD bool chol6_f64(double* A, double* b)
+{
+    const int m = 6;
+    for (int i = 0; i < m; ++i) {
+        for (int j = 0; j <= i; ++j) {
+            double s = A[i * m + j];
+            for (int k = 0; k < j; ++k) s -= A[i * m + k] * A[j * m + k];
+            if (i == j) {
+                if (!(s > 0.0)) return false;
+                A[i * m + i] = sqrt(s);
+            } else {
+                A[i * m + j] = s / A[j * m + j];
+            }
+        }
+    }
+    for (int i = 0; i < m; ++i) {
+        double s = b[i];
+        for (int k = 0; k < i; ++k) s -= A[i * m + k] * b[k];
+        b[i] = s / A[i * m + i];
+    }
+    for (int i = m - 1; i >= 0; --i) {
+        double s = b[i];
+        for (int k = i + 1; k < m; ++k) s -= A[k * m + i] * b[k];
+        b[i] = s / A[i * m + i];
+    }
+    return true;
+}
+
+// the small-angle increment of sensor_pose_estimation.cu:406-425,
+// x = (beta, gamma, alpha, tx, ty, tz)
+KF_HD void increment(const float* x, float* inc)
+{
+    inc[0] = 1.0f;  inc[1] = x[2];  inc[2] = -x[1]; inc[3] = x[3];
+    inc[4] = -x[2]; inc[5] = 1.0f;  inc[6] = x[0];  inc[7] = x[4];
+    inc[8] = x[1];  inc[9] = -x[0]; inc[10] = 1.0f; inc[11] = x[5];
+    inc[12] = 0.0f; inc[13] = 0.0f; inc[14] = 0.0f; inc[15] = 1.0f;
+}
+
+}  // namespace kf

@@ -1,0 +1,451 @@
+// Projective TSDF integration (projective_tsdf.cu:5-140) and Amanatides-Woo ray
+// casting (voxel_traversal.cu:4-424) over the device-resident volume.
+//
+// Integration keeps the reference's per-voxel arithmetic operation for operation, but
+// (a) voxel centres are computed from the index instead of read from three coordinate
+// arrays, (b) everything that depends only on the frame or on the pixel a voxel lands
+// in (T^-1, the in-front axis, the measured point's distance along the pixel ray and
+// 1/|R lambda|) is computed once (integrate_prep) and looked up, and (c) a voxel's
+// value and weight are read and written only when the voxel is updated.  The grid is
+// walked one thread per (x, y) column segment with x fastest, so a warp's updates are
+// 32 consecutive voxels.
+#include "kf_kernels.h"
+
+namespace kf {
+
+namespace {
+
+struct VolF32 {
+    float* t;
+    float* w;
+    __device__ __forceinline__ void load(size_t i, float& tv, float& wv) const
+    {
+        tv = t[i];
+        wv = w[i];
+    }
+    __device__ __forceinline__ void store(size_t i, float tv, float wv) const
+    {
+        t[i] = tv;
+        w[i] = wv;
+    }
+};
+
+struct VolF16 {
+    __half2* p;
+    __device__ __forceinline__ void load(size_t i, float& tv, float& wv) const
+    {
+        const float2 v = __half22float2(p[i]);
+        tv = v.x;
+        wv = v.y;
+    }
+    __device__ __forceinline__ void store(size_t i, float tv, float wv) const { p[i] = __floats2half2_rn(tv, wv); }
+};
+
+struct ViewF32 {
+    const float* t;
+    __device__ __forceinline__ float value(size_t i) const { return __ldg(t + i); }
+};
+
+struct ViewF16 {
+    const __half2* p;
+    __device__ __forceinline__ float value(size_t i) const
+    {
+        return __half2float(__low2half(__ldg(p + i)));
+    }
+};
+
+// Per pixel (u, v) (1-based): the quantities of projective_tsdf.cu:39-95 that depend
+// only on the pixel and the pose.  tab = (predicted_depth or NaN where the depth is
+// 0, 1 / |ray direction|).  Thread 0 also stores T^-1 (cv::Mat::inv, :149) and the
+// in-front axis (:57-71).
+__global__ void __launch_bounds__(256) integrate_prep_kernel(const float* __restrict__ depth, float2* __restrict__ tab,
+                                                             Camera cam, State* st)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const float* K = cam.K;
+    const float* Ki = cam.Ki;
+    float T[16];
+#pragma unroll
+    for (int k = 0; k < 16; ++k) T[k] = st->T[k];
+    if (i == 0) {
+        inv4(T, st->Tinv);
+        const float3 ca = mul3(Ki, make_float3(K[5], K[2], 1.f));
+        const float3 cb = make_float3(2 * (Ki[0] * K[5] + Ki[1] * K[2] + Ki[2] * 1.f),
+                                      2 * (Ki[3] * K[5] + Ki[4] * K[2] + Ki[5] * 1.f),
+                                      2 * (Ki[6] * K[5] + Ki[7] * K[2] + Ki[8] * 1.f));
+        const float3 ga = xform(T, ca), gb = xform(T, cb);
+        st->axis[0] = gb.x - ga.x;
+        st->axis[1] = gb.y - ga.y;
+        st->axis[2] = gb.z - ga.z;
+    }
+    if (i >= cam.H * cam.W) return;
+    const int u = i % cam.W + 1, v = i / cam.W + 1;
+    const float3 lam = make_float3(Ki[0] * (float)u + Ki[1] * (float)v + Ki[2] * 1.f,
+                                   Ki[3] * (float)u + Ki[4] * (float)v + Ki[5] * 1.f,
+                                   Ki[6] * (float)u + Ki[7] * (float)v + Ki[8] * 1.f);
+    const float3 rs = xform(T, lam);
+    const float3 rd = make_float3(T[0] * 2 * lam.x + T[1] * 2 * lam.y + T[2] * 2 * lam.z + T[3],
+                                  T[4] * 2 * lam.x + T[5] * 2 * lam.y + T[6] * 2 * lam.z + T[7],
+                                  T[8] * 2 * lam.x + T[9] * 2 * lam.y + T[10] * 2 * lam.z + T[11]);
+    const float3 dir = make_float3(rd.x - rs.x, rd.y - rs.y, rd.z - rs.z);
+    const float mag = sqrtf(dir.x * dir.x + dir.y * dir.y + dir.z * dir.z);
+    const float D = depth[i];
+    const float3 pt = xform(T, make_float3(D * lam.x, D * lam.y, D * lam.z));
+    const float3 rel = make_float3(pt.x - T[3], pt.y - T[7], pt.z - T[11]);
+    const float dist = sqrtf(rel.x * rel.x + rel.y * rel.y + rel.z * rel.z);
+    const float pd = dist / mag;
+    tab[i] = make_float2(D != 0 ? pd : qnan(), 1.f / mag);
+}
+
+constexpr int kIntTx = 32, kIntTy = 8;
+
+template <class Vol, bool FIRST>
+__global__ void __launch_bounds__(kIntTx* kIntTy) integrate_kernel(Vol vol, const float2* __restrict__ tab,
+                                                                   const State* __restrict__ st, Grid g, float fx,
+                                                                   float fy, float cx, float cy, int H, int W,
+                                                                   int zchunk, long long skip_from)
+{
+    const int x = blockIdx.x * kIntTx + threadIdx.x;
+    const int y = blockIdx.y * kIntTy + threadIdx.y;
+    if (x >= g.dx || y >= g.dy) return;
+    const int z0 = blockIdx.z * zchunk;
+    const int z1 = min(z0 + zchunk, g.dz);
+    float ti[12];
+#pragma unroll
+    for (int k = 0; k < 12; ++k) ti[k] = st->Tinv[k];
+    const float tx = st->T[3], ty = st->T[7], tz = st->T[11];
+    const float ax = st->axis[0], ay = st->axis[1], az = st->axis[2];
+    const float vcx = centre(x, g.sx, g.vd), vcy = centre(y, g.sy, g.vd);
+    // the first two products of each row of T^-1 c and of the in-front dot product and
+    // |c - t|^2 are the same along the column (left-to-right evaluation)
+    const float a0 = ti[0] * vcx + ti[1] * vcy;
+    const float a1 = ti[4] * vcx + ti[5] * vcy;
+    const float a2 = ti[8] * vcx + ti[9] * vcy;
+    const float tdx = vcx - tx, tdy = vcy - ty;
+    const float f0 = ax * tdx + ay * tdy;
+    const float m0 = tdx * tdx + tdy * tdy;
+    const long long rbase = ((long long)x * g.dy + y) * g.dz;
+    const size_t zstride = (size_t)g.dx * g.dy;
+    size_t lin = ((size_t)z0 * g.dy + y) * g.dx + x;
+    for (int z = z0; z < z1; ++z, lin += zstride) {
+        // the reference's guard compares the thread index with the voxel count in float
+        if (rbase + z >= skip_from) continue;
+        const float vcz = centre(z, g.sz, g.vd);
+        const float lx = (a0 + ti[2] * vcz) + ti[3];
+        const float ly = (a1 + ti[6] * vcz) + ti[7];
+        const float lz = (a2 + ti[10] * vcz) + ti[11];
+        // K (lx, ly, lz) with K's structural zeros dropped; adding a 0 product changes at
+        // most the sign of a zero result, which projects to pixel 0 and is rejected
+        // either way
+        const float px = fx * lx + cx * lz;
+        const float py = fy * ly + cy * lz;
+        const int u = (int)roundf(px / lz);
+        const int v = (int)roundf(py / lz);
+        if (u < 1 || u > W || v < 1 || v > H) continue;
+        const float2 e = __ldg(tab + (v - 1) * W + (u - 1));
+        if (isnan(e.x)) continue;
+        const float tdz = vcz - tz;
+        const float front = f0 + az * tdz;
+        if (!(front > 0)) continue;
+        const float tm = sqrtf(m0 + tdz * tdz);
+        const float frk = e.x - e.y * tm;
+        const bool ahead = frk > 0 && frk <= g.sdf_max;
+        const bool behind = frk <= 0 && frk >= g.sdf_min;
+        if (!ahead && !behind) continue;
+        const float f = ahead ? fminf(1.f, frk / g.trunc) : fmaxf(-1.f, frk / g.trunc);
+        if (FIRST) {
+            vol.store(lin, f, 1.0f);
+        } else {
+            float t, w;
+            vol.load(lin, t, w);
+            if (isnan(t)) t = 0.0f;
+            if (isnan(w)) w = 0.0f;
+            vol.store(lin, (w * t + 1.0f * f) / (w + 1.0f), w + 1.0f);
+        }
+    }
+}
+
+// Ray_Box_Intersection, voxel_traversal.cu:4-73
+__device__ __forceinline__ float slab_entry(bool& inside, float3 d, float3 lo, float3 hi, float3 o)
+{
+    float t0, t1, ty0, ty1, tz0, tz1;
+    if (d.x >= 0) {
+        t0 = (lo.x - o.x) / d.x;
+        t1 = (hi.x - o.x) / d.x;
+    } else {
+        t0 = (hi.x - o.x) / d.x;
+        t1 = (lo.x - o.x) / d.x;
+    }
+    if (d.y >= 0) {
+        ty0 = (lo.y - o.y) / d.y;
+        ty1 = (hi.y - o.y) / d.y;
+    } else {
+        ty0 = (hi.y - o.y) / d.y;
+        ty1 = (lo.y - o.y) / d.y;
+    }
+    if ((t0 > ty1) || (ty0 > t1)) {
+        inside = false;
+        return -1;
+    }
+    if (ty0 > t0) t0 = ty0;
+    if (ty1 < t1) t1 = ty1;
+    if (d.z >= 0) {
+        tz0 = (lo.z - o.z) / d.z;
+        tz1 = (hi.z - o.z) / d.z;
+    } else {
+        tz0 = (hi.z - o.z) / d.z;
+        tz1 = (lo.z - o.z) / d.z;
+    }
+    if ((t0 > tz1) || (tz0 > t1)) {
+        inside = false;
+        return -1;
+    }
+    if (tz0 > t0) t0 = tz0;
+    inside = true;
+    return t0;
+}
+
+// One ray of Voxel_Traversal (voxel_traversal.cu:90-422).  The axis records XY..ZY
+// start at 0, so a zero crossing met before the ray has stepped along every axis is
+// not a hit (the reference leaves them uninitialised; zero is what g++ -O2 gives).
+template <class View>
+__device__ __forceinline__ void trace(const View& vol, float X, float Y, float D, const float* Ki, const float* T,
+                                      const Grid& g, float c_flip, float4& op, float4& on, int& oh)
+{
+    const int L = g.dx, Wd = g.dy, Hz = g.dz;
+    const float vd = g.vd;
+    const float3 lo = make_float3((float)(g.sx * vd), (float)(g.sy * vd), (float)(g.sz * vd));
+    const float3 hi = make_float3((float)((g.sx + L) * vd), (float)((g.sy + Wd) * vd), (float)((g.sz + Hz) * vd));
+    const float3 lam = make_float3(Ki[0] * X + Ki[1] * Y + Ki[2] * 1.f, Ki[3] * X + Ki[4] * Y + Ki[5] * 1.f,
+                                   Ki[6] * X + Ki[7] * Y + Ki[8] * 1.f);
+    const float ln = sqrtf(lam.x * lam.x + lam.y * lam.y + lam.z * lam.z);
+    // start truncated_distance before the measurement (:99-106)
+    const float sc = (ln * D - g.trunc) / ln;
+    const float3 sl = make_float3(sc * lam.x, sc * lam.y, sc * lam.z);
+    const float3 org = make_float3(T[0] * sl.x + T[1] * sl.y + T[2] * sl.z + T[3] * 1.f,
+                                   T[4] * sl.x + T[5] * sl.y + T[6] * sl.z + T[7] * 1.f,
+                                   T[8] * sl.x + T[9] * sl.y + T[10] * sl.z + T[11] * 1.f);
+    const float3 cam = make_float3(T[3], T[7], T[11]);
+    const float3 lg = make_float3(T[0] * lam.x + T[1] * lam.y + T[2] * lam.z + T[3] * 1.f,
+                                  T[4] * lam.x + T[5] * lam.y + T[6] * lam.z + T[7] * 1.f,
+                                  T[8] * lam.x + T[9] * lam.y + T[10] * lam.z + T[11] * 1.f);
+    const float3 dir = normalized(make_float3(lg.x - cam.x, lg.y - cam.y, lg.z - cam.z));
+
+    bool inside = false;
+    float tmin = slab_entry(inside, dir, lo, hi, org);
+    if (!inside) return;
+    if (tmin < 0) tmin = 0;
+    const float3 s = make_float3(org.x + tmin * dir.x, org.y + tmin * dir.y, org.z + tmin * dir.z);
+    const float3 box = make_float3(hi.x - lo.x, hi.y - lo.y, hi.z - lo.z);
+    int ix = (int)floorf(((s.x - lo.x) / box.x) * L) + 1;
+    int iy = (int)floorf(((s.y - lo.y) / box.y) * Wd) + 1;
+    int iz = (int)floorf(((s.z - lo.z) / box.z) * Hz) + 1;
+    int XY = 0, XZ = 0, YX = 0, YZ = 0, ZX = 0, ZY = 0;
+    if (ix == L + 1) ix = ix - 1;
+    if (iy == Wd + 1) iy = iy - 1;
+    if (iz == Hz + 1) iz = iz - 1;
+    float tvx, tvy, tvz, sx, sy, sz;
+    if (dir.x >= 0) {
+        tvx = (float)(ix) / L;
+        sx = 1;
+    } else {
+        tvx = (float)(ix - 1) / L;
+        sx = -1;
+    }
+    if (dir.y >= 0) {
+        tvy = (float)(iy) / Wd;
+        sy = 1;
+    } else {
+        tvy = (float)(iy - 1) / Wd;
+        sy = -1;
+    }
+    if (dir.z >= 0) {
+        tvz = (float)(iz) / Hz;
+        sz = 1;
+    } else {
+        tvz = (float)(iz - 1) / Hz;
+        sz = -1;
+    }
+    const float3 vmax = make_float3(lo.x + tvx * box.x, lo.y + tvy * box.y, lo.z + tvz * box.z);
+    float3 tm = make_float3(tmin + ((vmax.x - s.x) / dir.x), tmin + ((vmax.y - s.y) / dir.y),
+                            tmin + ((vmax.z - s.z) / dir.z));
+    const float3 td = make_float3(vd / fabsf(dir.x), vd / fabsf(dir.y), vd / fabsf(dir.z));
+    const float fL = (float)L, fW = (float)Wd, fH = (float)Hz;
+    const size_t ys = (size_t)L, zs = (size_t)L * Wd;
+    auto lin = [&](int a, int b, int c) -> size_t { return (size_t)c * zs + (size_t)b * ys + (size_t)a; };
+
+    float prev = 0.0f;
+    // every iteration moves one index one step in a fixed direction, so the walk ends
+    // within L + Wd + Hz iterations; the bound only makes that explicit
+    for (int guard = 0; guard < L + Wd + Hz + 4; ++guard) {
+        if (!(ix < (fL - 1) && ix > 0 && iy < (fW - 1) && iy > 0 && iz < (fH - 1) && iz > 0)) break;
+        const float cur = vol.value(lin(ix - 1, iy - 1, iz - 1));
+        if (isnan(cur) && prev < 0.f) break;
+        if (cur < 0.f && isnan(prev)) break;
+        if (cur > 0.f && prev < 0.f) break;
+        if (cur < 0.f && prev > 0.f) {
+            const int xn = (ix - 1) - 1, xp = (ix - 1) + 1;
+            const int yn = (iy - 1) - 1, yp = (iy - 1) + 1;
+            const int zn = (iz - 1) - 1, zp = (iz - 1) + 1;
+            // :233-282; recorded indices are checked against the stepped axis' extent
+            if (xn >= L || xn < 0 || xp >= L || xp < 0) break;
+            if ((XY - 1) >= L || (XY - 1) < 0 || (XZ - 1) >= L || (XZ - 1) < 0) break;
+            if (yn >= Wd || yn < 0 || yp >= Wd || yp < 0) break;
+            if ((YX - 1) >= Wd || (YX - 1) < 0 || (YZ - 1) >= Wd || (YZ - 1) < 0) break;
+            if (zn >= Hz || zn < 0 || zp >= Hz || zp < 0) break;
+            if ((ZX - 1) >= Hz || (ZX - 1) < 0 || (ZY - 1) >= Hz || (ZY - 1) < 0) break;
+            // the recorded indices are in range for their own axes (they were loop
+            // positions), so every neighbour below lies inside the grid
+            const float v_xnp = vol.value(lin(xn, XY - 1, XZ - 1));
+            const float v_xpp = vol.value(lin(xp, XY - 1, XZ - 1));
+            const float v_ynp = vol.value(lin(YX - 1, yn, YZ - 1));
+            const float v_ypp = vol.value(lin(YX - 1, yp, YZ - 1));
+            const float v_znp = vol.value(lin(ZX - 1, ZY - 1, zn));
+            const float v_zpp = vol.value(lin(ZX - 1, ZY - 1, zp));
+            if (isnan(v_xnp) || isnan(v_xpp) || isnan(v_ynp) || isnan(v_ypp) || isnan(v_znp) || isnan(v_zpp) ||
+                isnan(cur))
+                break;
+            const float v_xnn = vol.value(lin(ix - 2, iy - 1, iz - 1));
+            const float v_xpn = vol.value(lin(ix, iy - 1, iz - 1));
+            const float v_ynn = vol.value(lin(ix - 1, iy - 2, iz - 1));
+            const float v_ypn = vol.value(lin(ix - 1, iy, iz - 1));
+            const float v_znn = vol.value(lin(ix - 1, iy - 1, iz - 2));
+            const float v_zpn = vol.value(lin(ix - 1, iy - 1, iz));
+            if (isnan(v_xnn) || isnan(v_xpn) || isnan(v_ynn) || isnan(v_ypn) || isnan(v_znn) || isnan(v_zpn)) break;
+            float3 sp;
+            // per-axis linear zero crossing (:318-349)
+            if (dir.x > 0)
+                sp.x = centre(xn, g.sx, vd) + vd * (fabsf(v_xnp) / (fabsf(v_xnp - cur)));
+            else
+                sp.x = centre(xp, g.sx, vd) - vd * (fabsf(v_xpp) / (fabsf(v_xpp - cur)));
+            if (dir.y > 0)
+                sp.y = centre(yn, g.sy, vd) + vd * (fabsf(v_ynp) / (fabsf(v_ynp - cur)));
+            else
+                sp.y = centre(yp, g.sy, vd) - vd * (fabsf(v_ypp) / (fabsf(v_ypp - cur)));
+            if (dir.z > 0)
+                sp.z = centre(zn, g.sz, vd) + vd * (fabsf(v_znp) / (fabsf(v_znp - cur)));
+            else
+                sp.z = centre(zp, g.sz, vd) - vd * (fabsf(v_zpp) / (fabsf(v_zpp - cur)));
+            const float3 nr = make_float3((v_xpn - v_xnn) / 2.0f, (v_ypn - v_ynn) / 2.0f, (v_zpn - v_znn) / 2.0f);
+            const float3 va = normalized(make_float3(cam.x - sp.x, cam.y - sp.y, cam.z - sp.z));
+            float3 vb = normalized(nr);
+            const float ct = va.x * vb.x + va.y * vb.y + va.z * vb.z;
+            if (ct < c_flip) vb = make_float3(-vb.x, -vb.y, -vb.z);
+            op = make_float4(sp.x, sp.y, sp.z, 0.f);
+            on = make_float4(vb.x, vb.y, vb.z, 0.f);
+            oh = ((ix - 1) * Wd + (iy - 1)) * Hz + (iz - 1);
+            return;
+        }
+        prev = cur;
+        // Amanatides-Woo step (:384-417)
+        if (tm.x < tm.y) {
+            if (tm.x < tm.z) {
+                ix = ix + sx;
+                XY = iy;
+                XZ = iz;
+                tm.x = tm.x + td.x;
+            } else {
+                iz = iz + sz;
+                ZX = ix;
+                ZY = iy;
+                tm.z = tm.z + td.z;
+            }
+        } else {
+            if (tm.y < tm.z) {
+                iy = iy + sy;
+                YX = ix;
+                YZ = iz;
+                tm.y = tm.y + td.y;
+            } else {
+                iz = iz + sz;
+                ZX = ix;
+                ZY = iy;
+                tm.z = tm.z + td.z;
+            }
+        }
+    }
+}
+
+constexpr int kRayTile = 16;
+
+// 256 threads per 16x16 pixel tile; each warp covers an 8x4 sub-tile so that its rays
+// walk neighbouring voxels.
+template <class View>
+__global__ void __launch_bounds__(256) raycast_kernel(View vol, const float* __restrict__ depth,
+                                                      float4* __restrict__ pv, float4* __restrict__ pn,
+                                                      int32_t* __restrict__ hit, Camera cam, Grid g,
+                                                      const State* __restrict__ st)
+{
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int px = blockIdx.x * kRayTile + (w & 1) * 8 + (lane & 7);
+    const int py = blockIdx.y * kRayTile + (w >> 1) * 4 + (lane >> 3);
+    if (px >= cam.W || py >= cam.H) return;
+    const int i = py * cam.W + px;
+    float4 op = make_float4(0.f, 0.f, 0.f, 0.f), on = op;
+    int oh = -1;
+    const float D = depth[i];
+    if (D != 0) {
+        float T[12];
+#pragma unroll
+        for (int k = 0; k < 12; ++k) T[k] = st->T[k];
+        trace(vol, (float)px + 1.0f, (float)py + 1.0f, D, cam.Ki, T, g, st->c_flip, op, on, oh);
+    }
+    pv[i] = op;
+    pn[i] = on;
+    if (hit) hit[i] = oh;
+}
+
+}  // namespace
+
+void launch_integrate_prep(const float* depth, float2* tab, const Camera& cam, State* st, cudaStream_t s)
+{
+    const int n = cam.H * cam.W;
+    integrate_prep_kernel<<<(n + 255) / 256, 256, 0, s>>>(depth, tab, cam, st);
+}
+
+namespace {
+constexpr int kZChunk = 16;
+
+template <class Vol>
+void integrate_launch(Vol vol, const float2* tab, const State* st, const Grid& g, const Camera& cam,
+                      long long skip_from, bool first, cudaStream_t s)
+{
+    dim3 block(kIntTx, kIntTy);
+    dim3 grid((g.dx + kIntTx - 1) / kIntTx, (g.dy + kIntTy - 1) / kIntTy, (g.dz + kZChunk - 1) / kZChunk);
+    const float fx = cam.K[0], fy = cam.K[4], cx = cam.K[2], cy = cam.K[5];
+    if (first)
+        integrate_kernel<Vol, true><<<grid, block, 0, s>>>(vol, tab, st, g, fx, fy, cx, cy, cam.H, cam.W, kZChunk,
+                                                           skip_from);
+    else
+        integrate_kernel<Vol, false><<<grid, block, 0, s>>>(vol, tab, st, g, fx, fy, cx, cy, cam.H, cam.W, kZChunk,
+                                                            skip_from);
+}
+}  // namespace
+
+void launch_integrate_f32(float* tsdf, float* weight, const float2* tab, const State* st, const Grid& g,
+                          const Camera& cam, long long skip_from, bool first, cudaStream_t s)
+{
+    integrate_launch(VolF32{tsdf, weight}, tab, st, g, cam, skip_from, first, s);
+}
+
+void launch_integrate_f16(__half2* vol, const float2* tab, const State* st, const Grid& g, const Camera& cam,
+                          long long skip_from, bool first, cudaStream_t s)
+{
+    integrate_launch(VolF16{vol}, tab, st, g, cam, skip_from, first, s);
+}
+
+void launch_raycast_f32(const float* tsdf, const float* depth, float4* pv, float4* pn, int32_t* hit,
+                        const Camera& cam, const Grid& g, const State* st, cudaStream_t s)
+{
+    dim3 grid((cam.W + kRayTile - 1) / kRayTile, (cam.H + kRayTile - 1) / kRayTile);
+    raycast_kernel<<<grid, 256, 0, s>>>(ViewF32{tsdf}, depth, pv, pn, hit, cam, g, st);
+}
+
+void launch_raycast_f16(const __half2* vol, const float* depth, float4* pv, float4* pn, int32_t* hit,
+                        const Camera& cam, const Grid& g, const State* st, cudaStream_t s)
+{
+    dim3 grid((cam.W + kRayTile - 1) / kRayTile, (cam.H + kRayTile - 1) / kRayTile);
+    raycast_kernel<<<grid, 256, 0, s>>>(ViewF16{vol}, depth, pv, pn, hit, cam, g, st);
+}
+
+}  // namespace kf

@@ -1,0 +1,286 @@
+"""GPU parity: the CUDA library (through the C ABI) against the CPU oracle.
+
+Each stage gets identical inputs on both sides.  Gates (from the reference's
+tolerances): integer results bit for bit -- integration weight counts and the set of
+integrated voxels, ray-cast hit voxel indices, ICP correspondence pairings; floats
+within TSDF |d| <= 1e-6, points <= 1e-5 m (1e-2 mm), normals <= 1e-5, pose
+<= 1e-5 rad / 1e-5 m.
+"""
+import numpy as np
+import pytest
+
+import kinect_fusion_slam_gb300 as kf
+from conftest import grid_spec
+
+pytestmark = pytest.mark.gpu
+
+TSDF_TOL = 1e-6
+POINT_TOL_MM = 1e-2
+NORMAL_TOL = 1e-5
+ROT_TOL = 1e-5
+TRANS_TOL_MM = 1e-2
+
+
+def make_handle(seq, **kw):
+    g, cam = seq.cfg.grid, seq.cfg.camera
+    h = kf.Handle(kf.make_config(height=cam.height, width=cam.width, dims=g.dims, grid_start=g.start,
+                                 voxel_size=g.voxel_size, **kw))
+    K = seq.K
+    h.set_intrinsics(K[0, 0], K[1, 1], K[0, 2], K[1, 2])
+    return h
+
+
+def assert_volume_parity(tg, wg, to, wo):
+    assert np.array_equal(np.isnan(wg), np.isnan(wo)), "integrated voxel sets differ"
+    assert np.array_equal(np.isnan(tg), np.isnan(to))
+    m = ~np.isnan(wo)
+    assert np.array_equal(wg[m], wo[m]), "weight counts differ"
+    d = np.abs(tg[m] - to[m])
+    assert d.size == 0 or d.max() <= TSDF_TOL, d.max()
+
+
+def test_depth_and_vertex_map(oracle, small_seq):
+    seq, depths = small_seq
+    h = make_handle(seq)
+    Ki = oracle.inv3(seq.K)
+    for d in depths:
+        h.set_depth_u16(d)
+        dg = h.depth()
+        do = oracle.depth_ingest(d)
+        assert np.array_equal(dg, do)
+        out_g, mask_g = h.calculate_vertices_and_normals()
+        out_o, mask_o = oracle.vertex_normal(do, Ki)
+        assert np.array_equal(mask_g, mask_o)
+        assert np.abs(out_g[:2] - out_o[:2]).max() <= POINT_TOL_MM
+        assert np.abs(out_g[2:] - out_o[2:]).max() <= NORMAL_TOL
+        # same operations in the same order without FMA: expected to be bit-identical
+        assert np.array_equal(out_g.view(np.uint32), out_o.view(np.uint32))
+
+
+@pytest.mark.parametrize("frame_pair", [(0, 1), (1, 3)])
+def test_integration(oracle, small_seq, frame_pair):
+    seq, depths = small_seq
+    gs = grid_spec(seq.cfg.grid)
+    h = make_handle(seq)
+    K = seq.K
+    Ki = oracle.inv3(K)
+    to = np.full(gs.nvox, np.nan, np.float32)
+    wo = np.full(gs.nvox, np.nan, np.float32)
+    for n, k in enumerate(frame_pair):
+        T = seq.poses[k].astype(np.float32)
+        depth = oracle.depth_ingest(depths[k])
+        h.set_pose(T)
+        h.set_depth_f32(depth)
+        h.projective_tsdf(first=(n == 0))
+        oracle.integrate(gs, depth, K, Ki, T, oracle.inv4(T), to, wo, first=(n == 0))
+        tg, wg = h.volume()
+        assert_volume_parity(tg, wg, to, wo)
+    assert np.count_nonzero(~np.isnan(wo)) > 1000
+
+
+def test_raycast(oracle, small_seq):
+    seq, depths = small_seq
+    gs = grid_spec(seq.cfg.grid)
+    h = make_handle(seq)
+    K = seq.K
+    Ki = oracle.inv3(K)
+    to = np.full(gs.nvox, np.nan, np.float32)
+    wo = np.full(gs.nvox, np.nan, np.float32)
+    for n, k in enumerate([0, 1, 2]):
+        T = seq.poses[k].astype(np.float32)
+        oracle.integrate(gs, oracle.depth_ingest(depths[k]), K, Ki, T, oracle.inv4(T), to, wo, first=(n == 0))
+    h.set_volume(to, wo)
+    for k in [2, 3]:
+        T = seq.poses[k].astype(np.float32)
+        depth = oracle.depth_ingest(depths[k])
+        h.set_pose(T)
+        h.set_depth_f32(depth)
+        hit_g = h.ray_casting()
+        pred_g = h.predicted()
+        pred_o, hit_o = oracle.raycast(gs, depth, Ki, T, to)
+        assert np.array_equal(hit_g, hit_o), f"{int((hit_g != hit_o).sum())} hit indices differ"
+        assert (hit_o >= 0).sum() > 500
+        m = hit_o >= 0
+        assert np.abs(pred_g[:3][:, m] - pred_o[:3][:, m]).max() <= POINT_TOL_MM
+        nm = m & ~np.isnan(pred_o[3])
+        assert np.abs(pred_g[3:][:, nm] - pred_o[3:][:, nm]).max() <= NORMAL_TOL
+        assert np.array_equal(np.isnan(pred_g), np.isnan(pred_o))
+        assert np.all(pred_g[:, ~m] == 0)
+
+
+def test_flip_threshold(oracle, small_seq):
+    """The ray-cast normal flip uses a float threshold the device derives from its own
+    double acos; it must equal the threshold of the oracle's libm acos."""
+    seq, _ = small_seq
+    h = make_handle(seq)
+    c = np.float32(h.flip_threshold())
+    assert oracle.lib.kfo_raycast_flip(float(np.nextafter(c, np.float32(-1)))) == 1
+    assert oracle.lib.kfo_raycast_flip(float(c)) == 0
+
+
+def _icp_inputs(oracle, seq, depths, k_prev=0, k_cur=1):
+    gs = grid_spec(seq.cfg.grid)
+    K = seq.K
+    Ki = oracle.inv3(K)
+    to = np.full(gs.nvox, np.nan, np.float32)
+    wo = np.full(gs.nvox, np.nan, np.float32)
+    Tp = seq.poses[k_prev].astype(np.float32)
+    dp = oracle.depth_ingest(depths[k_prev])
+    oracle.integrate(gs, dp, K, Ki, Tp, oracle.inv4(Tp), to, wo, first=True)
+    pred6, _ = oracle.raycast(gs, dp, Ki, Tp, to)
+    dc = oracle.depth_ingest(depths[k_cur])
+    v5, mask = oracle.vertex_normal(dc, Ki)
+    cur6 = np.stack([v5[0], v5[1], dc, v5[2], v5[3], v5[4]])
+    return Tp, dc, cur6, mask, pred6
+
+
+def test_icp_association(oracle, small_seq):
+    seq, depths = small_seq
+    Tp, dc, cur6, mask, pred6 = _icp_inputs(oracle, seq, depths)
+    h = make_handle(seq)
+    h.set_depth_f32(dc)
+    h.calculate_vertices_and_normals()
+    h.set_predicted(pred6)
+    rng = np.random.default_rng(3)
+    for trial in range(3):
+        T = Tp.copy()
+        if trial:
+            T[:3, 3] += rng.normal(0, 3, 3).astype(np.float32)
+        F = oracle.matmul4(oracle.inv4(Tp), T)
+        n_g, sums_g, pair_g = h.icp_associate(F, T)
+        n_o, sums42, pair_o = oracle.icp_associate(seq.K, F, T, cur6, mask, pred6)
+        assert n_o > 200
+        assert n_g == n_o
+        assert np.array_equal(pair_g, pair_o), f"{int((pair_g != pair_o).sum())} pairings differ"
+        A = sums42[6:].reshape(6, 6)
+        ref27 = np.concatenate([sums42[:6], A[np.triu_indices(6)]])
+        scale = np.abs(ref27).max()
+        assert np.abs(sums_g - ref27).max() <= 1e-4 * scale
+
+
+def test_estimate_pose(oracle, small_seq):
+    seq, depths = small_seq
+    Tp, dc, cur6, mask, pred6 = _icp_inputs(oracle, seq, depths)
+    h = make_handle(seq)
+    h.set_pose(Tp)
+    h.set_depth_f32(dc)
+    h.calculate_vertices_and_normals()
+    h.set_predicted(pred6)
+    Tg = h.estimate_sensor_pose()
+    To, log = oracle.estimate_pose(seq.K, Tp, cur6, mask, pred6, iters=10)
+    nc, ok = h.icp_stats(10)
+    assert nc[0] == log["ncorr"][0]
+    assert np.abs(Tg[:3, :3] - To[:3, :3]).max() <= ROT_TOL
+    assert np.abs(Tg[:3, 3] - To[:3, 3]).max() <= TRANS_TOL_MM
+
+
+def test_bilateral(oracle, small_seq):
+    seq, depths = small_seq
+    h = make_handle(seq)
+    d = oracle.depth_ingest(depths[1])
+    h.set_depth_f32(d)
+    h.bilateral_filtering()
+    out_g = h.depth()
+    r, sd = 3, 4.5
+    yy, xx = np.mgrid[-r:r + 1, -r:r + 1].astype(np.float32)
+    spatial = np.exp((-(xx * xx + yy * yy) / np.float32(2 * sd * sd)).astype(np.float64)).astype(np.float32)
+    out_o = oracle.bilateral(d, spatial, r, 30.0)
+    assert np.abs(out_g - out_o).max() <= 1e-2
+
+
+def run_synced(oracle, seq, depths, h):
+    """Runs the GPU frame loop and, at every frame, the oracle's stages on the GPU's own
+    state at the start of that frame: the ICP pose must agree within tolerance, and
+    integration and ray casting at the GPU's pose must agree bit for bit.  Returns the
+    worst pose deviations."""
+    gs = grid_spec(seq.cfg.grid)
+    K = seq.K
+    Ki = oracle.inv3(K)
+    T = np.eye(4, dtype=np.float32)
+    d = oracle.depth_ingest(depths[0])
+    to = np.full(gs.nvox, np.nan, np.float32)
+    wo = np.full(gs.nvox, np.nan, np.float32)
+    h.initial_processing(depths[0])
+    oracle.integrate(gs, d, K, Ki, T, oracle.inv4(T), to, wo, first=True)
+    tg, wg = h.volume()
+    assert_volume_parity(tg, wg, to, wo)
+    worst = [0.0, 0.0]
+    for k in range(1, len(depths)):
+        pred_prev = h.predicted()
+        T_prev = h.pose()
+        tg_prev, wg_prev = tg, wg
+        h.incoming_frame(depths[k])
+        Tg = h.pose()
+        d = oracle.depth_ingest(depths[k])
+        v5, mask = oracle.vertex_normal(d, Ki)
+        cur6 = np.stack([v5[0], v5[1], d, v5[2], v5[3], v5[4]])
+        To, log = oracle.estimate_pose(K, T_prev, cur6, mask, pred_prev, iters=10)
+        nc, _ = h.icp_stats(10)
+        assert nc[0] == log["ncorr"][0], f"frame {k}: first-iteration correspondences differ"
+        worst[0] = max(worst[0], float(np.abs(Tg[:3, :3] - To[:3, :3]).max()))
+        worst[1] = max(worst[1], float(np.abs(Tg[:3, 3] - To[:3, 3]).max()))
+        # integration and ray cast at the GPU's pose, from the GPU's volume
+        to, wo = tg_prev.copy(), wg_prev.copy()
+        oracle.integrate(gs, d, K, Ki, Tg, oracle.inv4(Tg), to, wo, first=False)
+        tg, wg = h.volume()
+        assert_volume_parity(tg, wg, to, wo)
+        pred_o, hit_o = oracle.raycast(gs, d, Ki, Tg, tg)
+        hit_g = h.ray_casting()
+        assert np.array_equal(hit_g, hit_o), f"frame {k}: {int((hit_g != hit_o).sum())} hits differ"
+        m = hit_o >= 0
+        assert np.abs(h.predicted()[:3][:, m] - pred_o[:3][:, m]).max() <= POINT_TOL_MM
+    return worst
+
+
+def test_pipeline_small(oracle, small_seq):
+    seq, depths = small_seq
+    worst = run_synced(oracle, seq, depths, make_handle(seq))
+    print(f"small: worst per-frame pose deviation rot {worst[0]:.2e}, trans {worst[1]:.2e} mm")
+    assert worst[0] <= ROT_TOL and worst[1] <= TRANS_TOL_MM
+
+
+def test_pipeline_c0(oracle, c0_seq):
+    """Config c0 (640x480, 180x180x150 @ 20 mm), 20 frames, stage-synced."""
+    seq, depths = c0_seq
+    worst = run_synced(oracle, seq, depths, make_handle(seq))
+    print(f"c0: worst per-frame pose deviation rot {worst[0]:.2e}, trans {worst[1]:.2e} mm")
+    assert worst[0] <= ROT_TOL and worst[1] <= TRANS_TOL_MM
+
+
+def test_graph_and_eager_agree(small_seq):
+    seq, depths = small_seq
+    poses = []
+    for graphs in (1, 0):
+        h = make_handle(seq, use_graphs=graphs)
+        h.initial_processing(depths[0])
+        for k in range(1, len(depths)):
+            h.incoming_frame(depths[k])
+        poses.append(h.pose())
+        h.close()
+    assert np.array_equal(poses[0], poses[1])
+
+
+def test_invalid_arguments(small_seq):
+    seq, _ = small_seq
+    h = make_handle(seq)
+    with pytest.raises(kf.KinfuError):
+        h.set_pose(np.full((4, 4), np.nan, np.float32))
+    with pytest.raises(kf.KinfuError):
+        h.set_intrinsics(0.0, 525.0, 320.0, 240.0)
+    with pytest.raises(ValueError):
+        h.incoming_frame(np.zeros((3, 3), np.uint16))
+
+
+def test_empty_depth_frame(small_seq):
+    """An all-zero frame: nothing is integrated or hit, ICP finds no correspondences and
+    the pose stays (reference behaviour: cv::Cholesky fails on A = 0, b = 0)."""
+    seq, depths = small_seq
+    h = make_handle(seq)
+    h.initial_processing(depths[0])
+    T0 = h.pose()
+    zero = np.zeros_like(depths[0])
+    h.incoming_frame(zero)
+    assert np.array_equal(h.pose(), T0)
+    nc, ok = h.icp_stats(10)
+    assert np.all(nc == 0) and np.all(ok == 0)
+    assert np.all(h.ray_casting() == -1)
