@@ -258,7 +258,9 @@ def run_gb300(args, dist: Dist):
                           voxel_size=g.voxel_size, tsdf_storage=storage)
     h = kf.Handle(conf)
     h.set_intrinsics(K[0, 0], K[1, 1], K[0, 2], K[1, 2])
-    stream = torch.cuda.current_stream()
+    # a dedicated stream: torch's default stream is the legacy NULL stream (handle 0)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     h.set_stream(stream.cuda_stream)
     dev = torch.from_numpy(frames.view(np.int16)).cuda()
     fbytes = cam.height * cam.width * 2

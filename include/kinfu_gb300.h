@@ -47,6 +47,11 @@ typedef int kf_status;
 #define KF_ICP_FAIL_REFERENCE 0 /* as the reference: the raw A^T b is used as the increment */
 #define KF_ICP_FAIL_IDENTITY 1  /* skip the increment */
 
+/* summation order of the ICP normal equations (plain FP32 form) */
+#define KF_REDUCE_REFERENCE_ORDER 0 /* the reference's 64-pixel trees added in block order: sums
+                                       and poses bit-identical to the reference's arithmetic */
+#define KF_REDUCE_TREE 1            /* one-pass warp/block/grid tree: faster, sums agree to rounding */
+
 /* 6x6 reduction / solve precision */
 #define KF_SOLVE_REFERENCE 0 /* float sums, float-stored Cholesky (cv::Cholesky), float pose */
 #define KF_SOLVE_PRECISE 1   /* compensated float sums, FP64 Cholesky and FP64 pose composition */
@@ -66,6 +71,7 @@ typedef struct kf_config {
     float icp_distance;      /* mm correspondence gate (20: sensor_pose_estimation.cu:48) */
     float icp_angle_deg;     /* normal gate in degrees (30: sensor_pose_estimation.cu:69) */
     int icp_fail_mode;       /* KF_ICP_FAIL_* */
+    int icp_reduction;       /* KF_REDUCE_* (KF_SOLVE_PRECISE always uses a compensated tree) */
     int solve_mode;          /* KF_SOLVE_* */
     int tsdf_storage;        /* KF_TSDF_* */
     int bilateral;           /* 0 = off as in the reference loop (kinfu_pipeline.cpp:141-145) */

@@ -20,11 +20,12 @@ from pathlib import Path
 import numpy as np
 
 from . import _lib
-from ._lib import (KF_ICP_FAIL_IDENTITY, KF_ICP_FAIL_REFERENCE, KF_SOLVE_PRECISE, KF_SOLVE_REFERENCE, KF_TSDF_F16,
-                   KF_TSDF_F32, Config, KinfuError)
+from ._lib import (KF_ICP_FAIL_IDENTITY, KF_ICP_FAIL_REFERENCE, KF_REDUCE_REFERENCE_ORDER, KF_REDUCE_TREE,
+                   KF_SOLVE_PRECISE, KF_SOLVE_REFERENCE, KF_TSDF_F16, KF_TSDF_F32, Config, KinfuError)
 
 __all__ = ["KinfuPipeline", "Handle", "Config", "KinfuError", "make_config", "KF_TSDF_F32", "KF_TSDF_F16",
-           "KF_ICP_FAIL_REFERENCE", "KF_ICP_FAIL_IDENTITY", "KF_SOLVE_REFERENCE", "KF_SOLVE_PRECISE"]
+           "KF_ICP_FAIL_REFERENCE", "KF_ICP_FAIL_IDENTITY", "KF_SOLVE_REFERENCE", "KF_SOLVE_PRECISE",
+           "KF_REDUCE_REFERENCE_ORDER", "KF_REDUCE_TREE"]
 
 
 def make_config(**kw) -> Config:

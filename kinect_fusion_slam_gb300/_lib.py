@@ -28,6 +28,8 @@ KF_TSDF_F32 = 0
 KF_TSDF_F16 = 1
 KF_ICP_FAIL_REFERENCE = 0
 KF_ICP_FAIL_IDENTITY = 1
+KF_REDUCE_REFERENCE_ORDER = 0
+KF_REDUCE_TREE = 1
 KF_SOLVE_REFERENCE = 0
 KF_SOLVE_PRECISE = 1
 
@@ -57,6 +59,7 @@ class Config(C.Structure):
         ("icp_distance", C.c_float),
         ("icp_angle_deg", C.c_float),
         ("icp_fail_mode", C.c_int),
+        ("icp_reduction", C.c_int),
         ("solve_mode", C.c_int),
         ("tsdf_storage", C.c_int),
         ("bilateral", C.c_int),

@@ -39,6 +39,7 @@ struct kf_handle {
     __half2* d_vol16 = nullptr;
     State* d_state = nullptr;
     float* d_partials = nullptr;
+    int* d_groups = nullptr;  // ICP group flags / compacted group list
     float* d_mats = nullptr;  // F, T (debug association input) + sums output
     float* d_spatial = nullptr;
 
@@ -112,6 +113,10 @@ bool validate(const kf_config* c, std::string& why)
         why = "icp_iterations out of range [0, 64]";
         return false;
     }
+    if (c->icp_reduction != KF_REDUCE_REFERENCE_ORDER && c->icp_reduction != KF_REDUCE_TREE) {
+        why = "unknown icp_reduction";
+        return false;
+    }
     if (c->tsdf_storage != KF_TSDF_F32 && c->tsdf_storage != KF_TSDF_F16) {
         why = "unknown tsdf_storage";
         return false;
@@ -171,7 +176,7 @@ void enq_icp(kf_handle* h)
 {
     for (int it = 0; it < h->cfg.icp_iterations[0]; ++it)
         launch_icp_iteration(h->d_vmap, h->d_nmap, h->d_pv, h->d_pn, h->cam, h->icp, h->d_state, h->d_partials,
-                             h->stream);
+                             h->d_groups, h->stream);
 }
 
 void enq_integrate(kf_handle* h, bool first)
@@ -313,7 +318,8 @@ kf_status allocate(kf_handle* h)
     KF_TRY(dalloc(h, &h->d_pair, HW));
     KF_TRY(dalloc(h, &h->d_tab, HW));
     KF_TRY(dalloc(h, &h->d_state, 1));
-    KF_TRY(dalloc(h, &h->d_partials, (size_t)2 * icp_grid_blocks(h->cam.H, h->cam.W) * kIcpVals));
+    KF_TRY(dalloc(h, &h->d_partials, icp_scratch_floats(h->cam.H, h->cam.W)));
+    KF_TRY(dalloc(h, &h->d_groups, (size_t)icp_groups(h->cam.H, h->cam.W)));
     KF_TRY(dalloc(h, &h->d_mats, 64));
     KF_TRY(dalloc(h, &h->d_spatial, 15 * 15));
     if (h->cfg.tsdf_storage == KF_TSDF_F16) {
@@ -360,7 +366,8 @@ void free_all(kf_handle* h)
 {
     destroy_graphs(h);
     void* dev[] = {h->d_raw, h->d_depth, h->d_depth_tmp, h->d_vmap, h->d_nmap, h->d_pv, h->d_pn, h->d_hit,
-                   h->d_pair, h->d_tab, h->d_tsdf, h->d_weight, h->d_vol16, h->d_state, h->d_partials, h->d_mats,
+                   h->d_pair, h->d_tab, h->d_tsdf, h->d_weight, h->d_vol16, h->d_state, h->d_partials, h->d_groups,
+                   h->d_mats,
                    h->d_spatial};
     for (void* p : dev)
         if (p) cudaFree(p);
@@ -413,6 +420,7 @@ void kf_config_default(kf_config* c)
     c->icp_distance = 20.f;
     c->icp_angle_deg = 30.f;
     c->icp_fail_mode = KF_ICP_FAIL_REFERENCE;
+    c->icp_reduction = KF_REDUCE_REFERENCE_ORDER;
     c->solve_mode = KF_SOLVE_REFERENCE;
     c->tsdf_storage = KF_TSDF_F32;
     c->bilateral = 0;
@@ -452,7 +460,8 @@ kf_status kf_create(const kf_config* cfg, kf_handle** out)
     // the reference's intrinsics (kinfu_pipeline.cpp:14-24)
     set_camera(h, 524.639f, 523.503f, 316.625f, 256.2318f);
     h->icp = IcpParams{cfg->icp_distance, cfg->icp_angle_deg, cfg->icp_fail_mode,
-                       cfg->solve_mode == KF_SOLVE_PRECISE ? 1 : 0};
+                       cfg->solve_mode == KF_SOLVE_PRECISE ? 1 : 0,
+                       cfg->icp_reduction == KF_REDUCE_REFERENCE_ORDER ? 1 : 0};
     h->nvox = (size_t)cfg->dims[0] * cfg->dims[1] * cfg->dims[2];
     h->skip_from = float_guard_start(cfg->dims);
     kf_status s = KF_OK;
@@ -838,7 +847,8 @@ kf_status kf_icp_associate(kf_handle* h, const float F[16], const float T[16], i
     std::memcpy(mats + 16, T, sizeof(float) * 16);
     KF_CUDA(h, cudaMemcpyAsync(h->d_mats, mats, sizeof(mats), cudaMemcpyHostToDevice, h->stream));
     launch_icp_associate(h->d_vmap, h->d_nmap, h->d_pv, h->d_pn, h->cam, h->icp, h->d_mats, h->d_mats + 16,
-                         h->d_state, h->d_partials, h->d_mats + 32, pair ? h->d_pair : nullptr, h->stream);
+                         h->d_state, h->d_partials, h->d_groups, h->d_mats + 32, pair ? h->d_pair : nullptr,
+                         h->stream);
     KF_CHECK_LAUNCH(h);
     float sums[kIcpVals];
     KF_CUDA(h, cudaMemcpyAsync(sums, h->d_mats + 32, sizeof(sums), cudaMemcpyDeviceToHost, h->stream));

@@ -30,8 +30,9 @@ struct Camera {
 struct IcpParams {
     float dist;       // mm
     float angle_deg;  // degrees
-    int fail_mode;    // 0 reference (raw b), 1 identity
-    int precise;      // compensated sums + FP64 solve
+    int fail_mode;        // 0 reference (raw b), 1 identity
+    int precise;          // compensated sums + FP64 solve
+    int reference_order;  // sums in the reference's order (bit-identical to it)
 };
 
 // Per-handle device state, updated by the kernels so that a whole frame runs without

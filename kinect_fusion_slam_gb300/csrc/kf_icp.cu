@@ -157,6 +157,62 @@ __device__ __forceinline__ void block_reduce(Acc<PRECISE>& acc, float* sh_hi, fl
 
 __device__ __forceinline__ int tri(int r, int s) { return 6 + r * 6 - r * (r - 1) / 2 + (s - r); }
 
+// Solve the 6x6 system from the reduced sums, apply the small-angle increment to the
+// pose and prepare the next iteration (sensor_pose_estimation.cu:389-429).  One thread.
+template <bool PRECISE>
+__device__ void finish_iteration(State* st, const IcpParams& prm, const float* hi, const float* lo)
+{
+    const int it = st->iter;
+    for (int k = 0; k < kIcpVals; ++k) st->sums[k] = PRECISE ? hi[k] + lo[k] : hi[k];
+    bool ok;
+    if (!PRECISE) {
+        float A[36], x[6];
+        for (int r = 0; r < 6; ++r)
+            for (int s = r; s < 6; ++s) A[r * 6 + s] = A[s * 6 + r] = hi[tri(r, s)];
+        for (int r = 0; r < 6; ++r) x[r] = hi[r];
+        // cv::Cholesky; on failure the reference keeps b untouched and applies it
+        ok = chol6(A, x);
+        if (!ok && prm.fail_mode == 1)
+            for (int r = 0; r < 6; ++r) x[r] = 0.f;
+        float inc[16];
+        increment(x, inc);
+        mat4(inc, st->T, st->T);
+    } else {
+        double A[36], x[6];
+        for (int r = 0; r < 6; ++r)
+            for (int s = r; s < 6; ++s) A[r * 6 + s] = A[s * 6 + r] = (double)hi[tri(r, s)] + (double)lo[tri(r, s)];
+        for (int r = 0; r < 6; ++r) x[r] = (double)hi[r] + (double)lo[r];
+        ok = chol6_f64(A, x);
+        if (!ok) {
+            if (prm.fail_mode == 1)
+                for (int r = 0; r < 6; ++r) x[r] = 0.0;
+            else
+                for (int r = 0; r < 6; ++r) x[r] = (double)hi[r] + (double)lo[r];
+        }
+        // SE(3) composition in FP64: the same small-angle increment, applied to the FP64 pose
+        const double inc[16] = {1.0, x[2], -x[1], x[3], -x[2], 1.0, x[0], x[4],
+                                x[1], -x[0], 1.0, x[5], 0.0, 0.0, 0.0, 1.0};
+        double R[16];
+        for (int r = 0; r < 4; ++r)
+            for (int c = 0; c < 4; ++c) {
+                double acc = 0.0;
+                for (int k = 0; k < 4; ++k) acc += inc[r * 4 + k] * st->Td[k * 4 + c];
+                R[r * 4 + c] = acc;
+            }
+        for (int k = 0; k < 16; ++k) {
+            st->Td[k] = R[k];
+            st->T[k] = (float)R[k];
+        }
+    }
+    mat4(st->Tprev_inv, st->T, st->F);
+    if (it < kMaxIcpIters) {
+        st->ncorr[it] = (int32_t)(hi[kIcpVals - 1] + (PRECISE ? lo[kIcpVals - 1] : 0.f));
+        st->chol_ok[it] = ok ? 1 : 0;
+        for (int k = 0; k < 16; ++k) st->Tlog[it][k] = st->T[k];
+    }
+    st->iter = it + 1;
+}
+
 // MODE 0: one ICP iteration (F, T from the state; the last block updates the pose).
 // MODE 1: association + reduction at the given F, T; the last block writes the sums.
 template <bool PRECISE, int MODE>
@@ -225,56 +281,139 @@ __global__ void __launch_bounds__(kIcpBlock) icp_kernel(const float4* __restrict
         return;
     }
 
-    const int it = st->iter;
-    for (int k = 0; k < kIcpVals; ++k) st->sums[k] = PRECISE ? red_hi[k] + red_lo[k] : red_hi[k];
-    bool ok;
-    if (!PRECISE) {
-        float A[36], x[6];
-        for (int r = 0; r < 6; ++r)
-            for (int s = r; s < 6; ++s) A[r * 6 + s] = A[s * 6 + r] = red_hi[tri(r, s)];
-        for (int r = 0; r < 6; ++r) x[r] = red_hi[r];
-        // cv::Cholesky; on failure the reference keeps b untouched and applies it
-        ok = chol6(A, x);
-        if (!ok && prm.fail_mode == 1)
-            for (int r = 0; r < 6; ++r) x[r] = 0.f;
-        float inc[16];
-        increment(x, inc);
-        mat4(inc, st->T, st->T);
-    } else {
-        double A[36], x[6];
-        for (int r = 0; r < 6; ++r)
-            for (int s = r; s < 6; ++s)
-                A[r * 6 + s] = A[s * 6 + r] = (double)red_hi[tri(r, s)] + (double)red_lo[tri(r, s)];
-        for (int r = 0; r < 6; ++r) x[r] = (double)red_hi[r] + (double)red_lo[r];
-        ok = chol6_f64(A, x);
-        if (!ok) {
-            if (prm.fail_mode == 1)
-                for (int r = 0; r < 6; ++r) x[r] = 0.0;
-            else
-                for (int r = 0; r < 6; ++r) x[r] = (double)red_hi[r] + (double)red_lo[r];
-        }
-        // SE(3) composition in FP64: the same small-angle increment, applied to the FP64 pose
-        const double inc[16] = {1.0, x[2], -x[1], x[3], -x[2], 1.0, x[0], x[4],
-                                x[1], -x[0], 1.0, x[5], 0.0, 0.0, 0.0, 1.0};
-        double R[16];
-        for (int r = 0; r < 4; ++r)
-            for (int c = 0; c < 4; ++c) {
-                double s = 0.0;
-                for (int k = 0; k < 4; ++k) s += inc[r * 4 + k] * st->Td[k * 4 + c];
-                R[r * 4 + c] = s;
+    finish_iteration<PRECISE>(st, prm, red_hi, red_lo);
+}
+
+// ---- reference summation order ----------------------------------------------------
+// Sum_Array (sensor_pose_estimation.cu:225-245) reduces each plane in blocks of 64
+// consecutive pixels with the tree sdata[t] += sdata[t + s], s = 32, 16, ..., 1, and the
+// host then adds the 4800 block sums one after another in block order (:369-372).  Here
+// one warp owns a 64-pixel group: lane t holds pixel t and adds pixel t + 32 (the s = 32
+// step), then shuffles down by 16, 8, 4, 2, 1 -- the same additions on the same operands,
+// so each group sum is bit-identical to the reference's.  The last CTA then adds the
+// group sums in group order.  Groups without a correspondence sum to +0 in every term,
+// and adding +0 to a running sum that starts at +0 never changes it, so those groups are
+// skipped without changing a bit.
+constexpr int kExactWarps = 8;
+constexpr int kExactChunk = 128;
+
+__device__ __forceinline__ void add_terms(float (&v)[kIcpVals], const float (&a)[6], float b)
+{
+#pragma unroll
+    for (int r = 0; r < 6; ++r) v[r] = v[r] + a[r] * b;
+#pragma unroll
+    for (int r = 0; r < 6; ++r)
+#pragma unroll
+        for (int s = r; s < 6; ++s) v[tri(r, s)] = v[tri(r, s)] + a[r] * a[s];
+    v[kIcpVals - 1] = v[kIcpVals - 1] + 1.f;
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(kExactWarps * 32) icp_exact_kernel(
+    const float4* __restrict__ vmap, const float4* __restrict__ nmap, const float4* __restrict__ pv,
+    const float4* __restrict__ pn, Camera cam, IcpParams prm, State* st, const float* Fsrc, const float* Tsrc,
+    float* partials, int* list, int ngroups, float* sums_out, int32_t* pair)
+{
+    __shared__ float sF[16], sT[16];
+    __shared__ float chunk[kExactChunk * kIcpVals];
+    __shared__ int warp_count[kExactWarps];
+    __shared__ int is_last, list_len;
+    __shared__ float red[kIcpVals];
+    if (threadIdx.x < 16) {
+        sF[threadIdx.x] = Fsrc[threadIdx.x];
+        sT[threadIdx.x] = Tsrc[threadIdx.x];
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int n = cam.H * cam.W;
+    for (int grp = blockIdx.x * kExactWarps + warp; grp < ngroups; grp += gridDim.x * kExactWarps) {
+        float v[kIcpVals];
+#pragma unroll
+        for (int k = 0; k < kIcpVals; ++k) v[k] = 0.f;
+        for (int half = 0; half < 2; ++half) {
+            const int i = grp * 64 + half * 32 + lane;
+            if (i >= n) continue;
+            float a[6], b;
+            int j = -1;
+            const bool ok = associate(i, vmap, nmap, pv, pn, cam, sF, sT, prm.dist, prm.angle_deg, a, b, j);
+            if (MODE == 1 && pair) pair[i] = ok ? j : -1;
+            if (!ok) continue;
+            if (half == 0) {
+#pragma unroll
+                for (int k = 0; k < kIcpVals; ++k) v[k] = 0.f;
+                add_terms(v, a, b);  // v = terms of pixel t (0 + x == x exactly)
+            } else {
+                float w[kIcpVals];
+#pragma unroll
+                for (int k = 0; k < kIcpVals; ++k) w[k] = 0.f;
+                add_terms(w, a, b);
+#pragma unroll
+                for (int k = 0; k < kIcpVals; ++k) v[k] = v[k] + w[k];  // sdata[t] += sdata[t + 32]
             }
-        for (int k = 0; k < 16; ++k) {
-            st->Td[k] = R[k];
-            st->T[k] = (float)R[k];
+        }
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1)
+#pragma unroll
+            for (int k = 0; k < kIcpVals; ++k) v[k] = v[k] + __shfl_down_sync(0xffffffffu, v[k], off);
+        if (lane == 0) {
+            list[grp] = v[kIcpVals - 1] != 0.f ? 1 : 0;
+#pragma unroll
+            for (int k = 0; k < kIcpVals; ++k) partials[(size_t)grp * kIcpVals + k] = v[k];
+            __threadfence();
         }
     }
-    mat4(st->Tprev_inv, st->T, st->F);
-    if (it < kMaxIcpIters) {
-        st->ncorr[it] = (int32_t)(red_hi[kIcpVals - 1] + (PRECISE ? red_lo[kIcpVals - 1] : 0.f));
-        st->chol_ok[it] = ok ? 1 : 0;
-        for (int k = 0; k < 16; ++k) st->Tlog[it][k] = st->T[k];
+    __syncthreads();
+    if (threadIdx.x == 0) is_last = (atomicAdd(&st->ticket, 1u) == gridDim.x - 1);
+    __syncthreads();
+    if (!is_last) return;
+    __threadfence();
+
+    // compact the indices of groups with correspondences, in order, in place
+    if (threadIdx.x == 0) list_len = 0;
+    __syncthreads();
+    for (int base = 0; base < ngroups; base += kExactWarps * 32) {
+        const int g = base + threadIdx.x;
+        const int f = g < ngroups ? __ldcg(list + g) : 0;
+        const unsigned m = __ballot_sync(0xffffffffu, f);
+        if (lane == 0) warp_count[warp] = __popc(m);
+        __syncthreads();
+        int off = list_len;
+        for (int w = 0; w < warp; ++w) off += warp_count[w];
+        const int pos = off + __popc(m & ((1u << lane) - 1u));
+        __syncthreads();  // every thread has read its flag and list_len
+        if (f) list[pos] = g;
+        if (threadIdx.x == 0) {
+            int tot = 0;
+            for (int w = 0; w < kExactWarps; ++w) tot += warp_count[w];
+            list_len += tot;
+        }
+        __syncthreads();
     }
-    st->iter = it + 1;
+    __threadfence_block();
+    // serial sum of the group partials in group order, one lane per term
+    float sum = 0.f;
+    for (int base = 0; base < list_len; base += kExactChunk) {
+        const int cnt = min(kExactChunk, list_len - base);
+        for (int e = threadIdx.x; e < cnt * kIcpVals; e += kExactWarps * 32) {
+            const int row = e / kIcpVals, k = e % kIcpVals;
+            chunk[e] = __ldcg(partials + (size_t)list[base + row] * kIcpVals + k);
+        }
+        __syncthreads();
+        if (warp == 0 && lane < kIcpVals) {
+#pragma unroll 8
+            for (int r = 0; r < cnt; ++r) sum = sum + chunk[r * kIcpVals + lane];
+        }
+        __syncthreads();
+    }
+    if (warp == 0 && lane < kIcpVals) red[lane] = sum;
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    st->ticket = 0u;
+    if (MODE == 1) {
+        for (int k = 0; k < kIcpVals; ++k) sums_out[k] = red[k];
+        return;
+    }
+    finish_iteration<false>(st, prm, red, red);
 }
 
 // device addresses of State members, computed without dereferencing on the host
@@ -291,11 +430,33 @@ int blocks_for(int H, int W)
 
 int icp_grid_blocks(int H, int W) { return blocks_for(H, W); }
 
+int icp_groups(int H, int W) { return (H * W + 63) / 64; }
+
+size_t icp_scratch_floats(int H, int W)
+{
+    const size_t a = (size_t)2 * blocks_for(H, W) * kIcpVals;
+    const size_t b = (size_t)icp_groups(H, W) * kIcpVals;
+    return a > b ? a : b;
+}
+
+namespace {
+int exact_blocks(int H, int W)
+{
+    const int g = icp_groups(H, W);
+    return (g + kExactWarps - 1) / kExactWarps;
+}
+}  // namespace
+
 void launch_icp_iteration(const float4* vmap, const float4* nmap, const float4* pv, const float4* pn,
-                          const Camera& cam, const IcpParams& prm, State* st, float* partials, cudaStream_t s)
+                          const Camera& cam, const IcpParams& prm, State* st, float* partials, int* list,
+                          cudaStream_t s)
 {
     const int blocks = blocks_for(cam.H, cam.W);
-    if (prm.precise)
+    if (!prm.precise && prm.reference_order)
+        icp_exact_kernel<0><<<exact_blocks(cam.H, cam.W), kExactWarps * 32, 0, s>>>(
+            vmap, nmap, pv, pn, cam, prm, st, state_F(st), state_T(st), partials, list, icp_groups(cam.H, cam.W),
+            nullptr, nullptr);
+    else if (prm.precise)
         icp_kernel<true, 0><<<blocks, kIcpBlock, 0, s>>>(vmap, nmap, pv, pn, cam, prm, st, state_F(st),
                                                          state_T(st), partials, nullptr, nullptr);
     else
@@ -305,10 +466,13 @@ void launch_icp_iteration(const float4* vmap, const float4* nmap, const float4* 
 
 void launch_icp_associate(const float4* vmap, const float4* nmap, const float4* pv, const float4* pn,
                           const Camera& cam, const IcpParams& prm, const float* F, const float* T, State* st,
-                          float* partials, float* sums_out, int32_t* pair, cudaStream_t s)
+                          float* partials, int* list, float* sums_out, int32_t* pair, cudaStream_t s)
 {
     const int blocks = blocks_for(cam.H, cam.W);
-    if (prm.precise)
+    if (!prm.precise && prm.reference_order)
+        icp_exact_kernel<1><<<exact_blocks(cam.H, cam.W), kExactWarps * 32, 0, s>>>(
+            vmap, nmap, pv, pn, cam, prm, st, F, T, partials, list, icp_groups(cam.H, cam.W), sums_out, pair);
+    else if (prm.precise)
         icp_kernel<true, 1><<<blocks, kIcpBlock, 0, s>>>(vmap, nmap, pv, pn, cam, prm, st, F, T, partials, sums_out,
                                                          pair);
     else

@@ -26,13 +26,18 @@ void launch_bilateral(const float* depth, float* out, const float* spatial, int 
 // One ICP iteration: association + one-pass reduction + (last block) 6x6 solve and pose
 // update.  partials must hold icp_grid_blocks() * kIcpVals floats.
 int icp_grid_blocks(int H, int W);
+// 64-pixel groups of the reference-order reduction, and the scratch (floats) both
+// reductions need; list must hold icp_groups() ints
+int icp_groups(int H, int W);
+size_t icp_scratch_floats(int H, int W);
 void launch_icp_iteration(const float4* vmap, const float4* nmap, const float4* pv, const float4* pn,
-                          const Camera& cam, const IcpParams& prm, State* st, float* partials, cudaStream_t s);
+                          const Camera& cam, const IcpParams& prm, State* st, float* partials, int* list,
+                          cudaStream_t s);
 // Association + reduction only at the given F, T (device pointers to 16 floats each);
 // sums_out receives kIcpVals floats (27 sums + count), pair may be nullptr.
 void launch_icp_associate(const float4* vmap, const float4* nmap, const float4* pv, const float4* pn,
                           const Camera& cam, const IcpParams& prm, const float* F, const float* T, State* st,
-                          float* partials, float* sums_out, int32_t* pair, cudaStream_t s);
+                          float* partials, int* list, float* sums_out, int32_t* pair, cudaStream_t s);
 
 // per-pixel integration table + T^-1 and the in-front axis into st
 void launch_integrate_prep(const float* depth, float2* tab, const Camera& cam, State* st, cudaStream_t s);

@@ -154,8 +154,25 @@ def test_icp_association(oracle, small_seq):
         assert np.array_equal(pair_g, pair_o), f"{int((pair_g != pair_o).sum())} pairings differ"
         A = sums42[6:].reshape(6, 6)
         ref27 = np.concatenate([sums42[:6], A[np.triu_indices(6)]])
-        scale = np.abs(ref27).max()
-        assert np.abs(sums_g - ref27).max() <= 1e-4 * scale
+        # the reference's summation order: bit-identical sums
+        assert np.array_equal(sums_g.view(np.uint32), ref27.view(np.uint32))
+
+
+def test_icp_association_tree_order(oracle, small_seq):
+    """The one-pass tree reduction: same pairings, sums equal to rounding."""
+    seq, depths = small_seq
+    Tp, dc, cur6, mask, pred6 = _icp_inputs(oracle, seq, depths)
+    h = make_handle(seq, icp_reduction=kf.KF_REDUCE_TREE)
+    h.set_depth_f32(dc)
+    h.calculate_vertices_and_normals()
+    h.set_predicted(pred6)
+    F = oracle.matmul4(oracle.inv4(Tp), Tp)
+    n_g, sums_g, pair_g = h.icp_associate(F, Tp)
+    n_o, sums42, pair_o = oracle.icp_associate(seq.K, F, Tp, cur6, mask, pred6)
+    assert n_g == n_o and np.array_equal(pair_g, pair_o)
+    A = sums42[6:].reshape(6, 6)
+    ref27 = np.concatenate([sums42[:6], A[np.triu_indices(6)]])
+    assert np.abs(sums_g - ref27).max() <= 1e-4 * np.abs(ref27).max()
 
 
 def test_estimate_pose(oracle, small_seq):
@@ -168,10 +185,41 @@ def test_estimate_pose(oracle, small_seq):
     h.set_predicted(pred6)
     Tg = h.estimate_sensor_pose()
     To, log = oracle.estimate_pose(seq.K, Tp, cur6, mask, pred6, iters=10)
-    nc, ok = h.icp_stats(10)
+    nc, ok, Ts = h.icp_stats(10, poses=True)
+    assert np.array_equal(nc, log["ncorr"]) and np.array_equal(ok, log["chol_ok"])
+    # reference summation order + the same solve: every iteration's pose bit for bit
+    assert np.array_equal(Ts.view(np.uint32), log["poses"].view(np.uint32))
+    assert np.array_equal(Tg.view(np.uint32), To.view(np.uint32))
+
+
+def test_estimate_pose_tree_order(oracle, small_seq):
+    seq, depths = small_seq
+    Tp, dc, cur6, mask, pred6 = _icp_inputs(oracle, seq, depths)
+    h = make_handle(seq, icp_reduction=kf.KF_REDUCE_TREE)
+    h.set_pose(Tp)
+    h.set_depth_f32(dc)
+    h.calculate_vertices_and_normals()
+    h.set_predicted(pred6)
+    h.estimate_sensor_pose()
+    To, log = oracle.estimate_pose(seq.K, Tp, cur6, mask, pred6, iters=10)
+    nc, ok, Ts = h.icp_stats(10, poses=True)
     assert nc[0] == log["ncorr"][0]
-    assert np.abs(Tg[:3, :3] - To[:3, :3]).max() <= ROT_TOL
-    assert np.abs(Tg[:3, 3] - To[:3, 3]).max() <= TRANS_TOL_MM
+    # the first iteration sees identical inputs: its pose agrees to rounding
+    assert np.abs(Ts[0] - log["poses"][0]).max() <= 1e-5 * max(1.0, np.abs(To).max())
+
+
+def test_icp_fail_identity(small_seq):
+    """KF_ICP_FAIL_IDENTITY: a failed factorisation leaves the pose unchanged."""
+    seq, depths = small_seq
+    h = make_handle(seq, icp_fail_mode=kf.KF_ICP_FAIL_IDENTITY)
+    h.initial_processing(depths[0])
+    T = seq.poses[1].astype(np.float32)
+    T[:3, 3] += 5000.0  # far outside the scene: no correspondences, A = 0
+    h.set_pose(T)
+    h.incoming_frame(depths[1])
+    nc, ok = h.icp_stats(10)
+    assert np.all(nc == 0) and np.all(ok == 0)
+    assert np.array_equal(h.pose(), T)
 
 
 def test_bilateral(oracle, small_seq):
@@ -188,7 +236,7 @@ def test_bilateral(oracle, small_seq):
     assert np.abs(out_g - out_o).max() <= 1e-2
 
 
-def run_synced(oracle, seq, depths, h):
+def run_synced(oracle, seq, depths, h, exact=True):
     """Runs the GPU frame loop and, at every frame, the oracle's stages on the GPU's own
     state at the start of that frame: the ICP pose must agree within tolerance, and
     integration and ray casting at the GPU's pose must agree bit for bit.  Returns the
@@ -217,6 +265,8 @@ def run_synced(oracle, seq, depths, h):
         To, log = oracle.estimate_pose(K, T_prev, cur6, mask, pred_prev, iters=10)
         nc, _ = h.icp_stats(10)
         assert nc[0] == log["ncorr"][0], f"frame {k}: first-iteration correspondences differ"
+        if exact:
+            assert np.array_equal(Tg.view(np.uint32), To.view(np.uint32)), f"frame {k}: pose bits differ"
         worst[0] = max(worst[0], float(np.abs(Tg[:3, :3] - To[:3, :3]).max()))
         worst[1] = max(worst[1], float(np.abs(Tg[:3, 3] - To[:3, 3]).max()))
         # integration and ray cast at the GPU's pose, from the GPU's volume
@@ -240,11 +290,32 @@ def test_pipeline_small(oracle, small_seq):
 
 
 def test_pipeline_c0(oracle, c0_seq):
-    """Config c0 (640x480, 180x180x150 @ 20 mm), 20 frames, stage-synced."""
+    """Config c0 (640x480, 180x180x150 @ 20 mm), 20 frames, stage-synced, reference
+    summation order: poses bit for bit at every frame."""
     seq, depths = c0_seq
     worst = run_synced(oracle, seq, depths, make_handle(seq))
     print(f"c0: worst per-frame pose deviation rot {worst[0]:.2e}, trans {worst[1]:.2e} mm")
-    assert worst[0] <= ROT_TOL and worst[1] <= TRANS_TOL_MM
+    assert worst == [0.0, 0.0]
+
+
+def test_pipeline_free_running_c0(oracle, c0_seq):
+    """GPU and oracle each run the whole c0 sequence on their own: the same trajectory,
+    volume and prediction bit for bit."""
+    seq, depths = c0_seq
+    gs = grid_spec(seq.cfg.grid)
+    h = make_handle(seq)
+    o = oracle.pipeline(480, 640, gs, seq.K)
+    h.initial_processing(depths[0])
+    o.initial(depths[0])
+    for k in range(1, len(depths)):
+        h.incoming_frame(depths[k])
+        o.incoming(depths[k])
+        assert np.array_equal(h.pose().view(np.uint32), o.pose.view(np.uint32)), f"frame {k}"
+    tg, wg = h.volume()
+    to, wo = o.volume()
+    assert_volume_parity(tg, wg, to, wo)
+    pred_o, hit_o = o.prediction()
+    assert np.array_equal(h.ray_casting(), hit_o)
 
 
 def test_graph_and_eager_agree(small_seq):
