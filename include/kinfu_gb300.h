@@ -173,6 +173,29 @@ kf_status kf_icp_associate(kf_handle* h, const float F[16], const float T[16], i
  * computed on the device from its own acos at kf_create */
 kf_status kf_get_flip_threshold(kf_handle* h, float* c_flip);
 
+/* ---- allocation-free variant ------------------------------------------------------
+ * No counterpart in the reference.  One ICP association + normal-equation reduction
+ * (as kf_icp_associate, reference summation order) on caller-owned DEVICE buffers,
+ * for callers that cannot allocate device memory at this point -- a real-time loop
+ * that must not stall on cudaMalloc, or an application that hands out all GPU memory
+ * from its own pre-reserved pool.  It allocates nothing: its scratch is a static
+ * device array of about 0.55 MB that every GPU loading this library holds until exit.
+ *   height * width <= 640 * 480 (307200 pixels), else KF_ERR_UNSUPPORTED;
+ *   vmap:   H*W x 4 floats (vx, vy, vz, vertex mask), 16-byte aligned, device;
+ *   nmap:   H*W x 4 floats (nx, ny, nz, unused), 16-byte aligned, device;
+ *   pred_v, pred_n: the previous ray cast's points / normals, same layout, device;
+ *   K, F, T: host 3x3 / 4x4 row-major; dist_mm / angle_deg: the ICP gates (20, 30);
+ *   sums28: device, receives the 6 entries of A^T b, the 21 of the upper triangle of
+ *           A^T A row by row, and the correspondence count (as a float);
+ *   pair:   device H*W int32 (matched pixel index or -1), or NULL;
+ *   stream: cudaStream_t passed as void* (NULL = the default stream).
+ * Asynchronous on stream.  The first call on each device looks up the scratch array's
+ * device address (cudaGetSymbolAddress), so make that first call before any stream
+ * capture.  All calls share the scratch array: calls that overlap on the GPU race. */
+kf_status kf_icp_associate_noalloc(int height, int width, const float K[9], const float F[16], const float T[16],
+                                   const float* vmap, const float* nmap, const float* pred_v, const float* pred_n,
+                                   float dist_mm, float angle_deg, float* sums28, int32_t* pair, void* stream);
+
 /* ---- timing --------------------------------------------------------------------- */
 /* per-stage device time of the latest kf_incoming_frame (CUDA events, ms):
  * [0] depth+vertex, [1] ICP, [2] integration, [3] ray cast, [4] whole frame.

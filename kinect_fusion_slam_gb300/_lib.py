@@ -113,6 +113,8 @@ SIGNATURES = {
     "kf_enable_stage_timing": (C.c_int, [_H, C.c_int]),
     "kf_get_stage_times": (C.c_int, [_H, _f32p]),
     "kf_kernels_per_frame": (C.c_int, [_H, C.POINTER(C.c_int)]),
+    "kf_icp_associate_noalloc": (C.c_int, [C.c_int, C.c_int, _f32p, _f32p, _f32p, _vp, _vp, _vp, _vp, C.c_float,
+                                           C.c_float, _vp, _vp, _vp]),
 }
 
 _lib = None
