@@ -6,12 +6,13 @@
 // The pose never leaves the device during a frame: every kernel reads it from, and
 // the ICP's last block writes it to, the State block.
 #include <cmath>
+#include <cstddef>
 #include <cstdio>
 #include <cstring>
 #include <string>
 #include <vector>
 
-#include "../../include/kinfu_gb300.h"
+#include "kinfu_gb300.h"
 #include "kf_kernels.h"
 
 using namespace kf;
@@ -97,6 +98,10 @@ bool validate(const kf_config* c, std::string& why)
             why = "grid dimensions out of range";
             return false;
         }
+    if (c->icp_reduction == KF_REDUCE_REFERENCE_ORDER && (long long)c->height * c->width > 32768LL * 64) {
+        why = "the reference-order ICP reduction supports up to 2097152 pixels";
+        return false;
+    }
     if ((double)c->dims[0] * c->dims[1] * c->dims[2] > 2147483647.0) {
         why = "grid has more than 2^31-1 voxels (the reference indexes voxels with int)";
         return false;
@@ -468,6 +473,7 @@ kf_status kf_create(const kf_config* cfg, kf_handle** out)
     if (cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking) != cudaSuccess) s = KF_ERR_CUDA;
     h->stream = h->own_stream;
     if (s == KF_OK) s = allocate(h);
+    if (s == KF_OK) icp_prepare(h->cam.H, h->cam.W);
     if (s == KF_OK && cfg->bilateral) s = upload_spatial(h);
     if (s == KF_OK) s = reset_state(h);
     if (s != KF_OK) {
@@ -537,9 +543,16 @@ kf_status kf_get_pose(kf_handle* h, float T[16])
 {
     KF_HANDLE(h);
     if (!T) return fail(h, KF_ERR_INVALID_ARGUMENT, "null pose");
-    KF_CUDA(h, cudaMemcpyAsync(T, field_ptr<float>(h->d_state, offsetof(State, T)), sizeof(float) * 16,
-                               cudaMemcpyDeviceToHost, h->stream));
+    // T and the error flag are adjacent in State: one small copy reads both
+    constexpr size_t bytes = offsetof(State, error) + sizeof(int);
+    KF_CUDA(h, cudaMemcpyAsync(h->h_state, h->d_state, bytes, cudaMemcpyDeviceToHost, h->stream));
     KF_CUDA(h, cudaStreamSynchronize(h->stream));
+    std::memcpy(T, h->h_state->T, sizeof(float) * 16);
+    if (h->h_state->error) {
+        const int zero = 0;
+        cudaMemcpy(field_ptr<int>(h->d_state, offsetof(State, error)), &zero, sizeof(int), cudaMemcpyHostToDevice);
+        return fail(h, KF_ERR_CUDA, "a kernel's bounded wait for a bulk copy gave up; the pose was not updated");
+    }
     return KF_OK;
 }
 

@@ -39,6 +39,7 @@ struct IcpParams {
 // host round trips.
 struct State {
     float T[16];          // extrinsic_matrix: camera-to-world pose
+    int error;            // set by a kernel whose bounded wait gave up (read with T)
     float Tprev_inv[16];  // inverse of the pose at the start of the frame's ICP
     float F[16];          // Tprev_inv * T, the frame-to-frame transform of the iteration
     float Tinv[16];       // inverse of the pose used by integration

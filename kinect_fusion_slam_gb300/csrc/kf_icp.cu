@@ -213,6 +213,99 @@ __device__ void finish_iteration(State* st, const IcpParams& prm, const float* h
     st->iter = it + 1;
 }
 
+// The same solve and update as finish_iteration<false> with the work spread over the
+// 32 lanes of one warp (FP64 latency dominates this step on GB300): the Cholesky factor
+// is formed column by column -- each entry from the same operands in the same order as
+// cv::Cholesky's row-by-row loop, so every bit is the same -- and each entry of the two
+// 4x4 products is computed by its own lane.  All 32 lanes of the calling warp must call.
+__device__ void finish_iteration_warp(State* st, const IcpParams& prm, const float* sums)
+{
+    __shared__ float L[36], xb[6], inc[16], Tn[16];
+    __shared__ int fail;
+    const int lane = threadIdx.x & 31;
+    if (lane < 6) {
+        xb[lane] = sums[lane];
+        for (int c = 0; c <= lane; ++c) L[lane * 6 + c] = sums[tri(c, lane)];  // lower triangle of A
+    }
+    if (lane == 0) fail = 0;
+    __syncwarp();
+    for (int j = 0; j < 6; ++j) {
+        // lanes j..5 accumulate row lane's entry of column j in one instruction stream:
+        // the diagonal subtracts the double square of each float, the off-diagonal the
+        // float product (cv::Cholesky's two inner loops), selected per lane
+        double sd = 0.0;
+        const int row = lane < 6 ? lane : 5;
+        if (lane >= j && lane < 6) {
+            sd = L[row * 6 + j];
+            for (int k = 0; k < j; ++k) {
+                const double t = L[row * 6 + k];
+                const double d_diag = t * t;
+                const double d_off = (double)(L[row * 6 + k] * L[j * 6 + k]);
+                sd -= lane == j ? d_diag : d_off;
+            }
+        }
+        if (lane == j) {
+            if (sd < FLT_EPSILON)
+                fail = 1;
+            else
+                L[j * 6 + j] = (float)(1. / sqrt(sd));
+        }
+        __syncwarp();
+        if (fail) break;
+        if (lane > j && lane < 6) L[lane * 6 + j] = (float)(sd * L[j * 6 + j]);
+        __syncwarp();
+    }
+    const bool ok = !fail;
+    if (lane == 0) {
+        if (ok) {
+            for (int i = 0; i < 6; ++i) {
+                double sd = xb[i];
+                for (int k = 0; k < i; ++k) sd -= L[i * 6 + k] * xb[k];
+                xb[i] = (float)(sd * L[i * 6 + i]);
+            }
+            for (int i = 5; i >= 0; --i) {
+                double sd = xb[i];
+                for (int k = 5; k > i; --k) sd -= L[k * 6 + i] * xb[k];
+                xb[i] = (float)(sd * L[i * 6 + i]);
+            }
+        } else if (prm.fail_mode == 1) {
+            for (int i = 0; i < 6; ++i) xb[i] = 0.f;
+        }
+        increment(xb, inc);
+    }
+    __syncwarp();
+    // T <- Inc * T and F <- T_prev^-1 * T, one output entry per lane (kf::mat4's order)
+    if (lane < 16) {
+        const int r = lane >> 2, c = lane & 3;
+        double a = (double)inc[r * 4 + 0] * st->T[c];
+        a += (double)inc[r * 4 + 1] * st->T[4 + c];
+        a += (double)inc[r * 4 + 2] * st->T[8 + c];
+        a += (double)inc[r * 4 + 3] * st->T[12 + c];
+        Tn[lane] = (float)a;
+    }
+    __syncwarp();
+    if (lane < 16) {
+        st->T[lane] = Tn[lane];
+        const int r = lane >> 2, c = lane & 3;
+        double a = (double)st->Tprev_inv[r * 4 + 0] * Tn[c];
+        a += (double)st->Tprev_inv[r * 4 + 1] * Tn[4 + c];
+        a += (double)st->Tprev_inv[r * 4 + 2] * Tn[8 + c];
+        a += (double)st->Tprev_inv[r * 4 + 3] * Tn[12 + c];
+        st->F[lane] = (float)a;
+    }
+    const int it = st->iter;
+    if (it < kMaxIcpIters && lane < 16) st->Tlog[it][lane] = Tn[lane];
+    if (lane < kIcpVals) st->sums[lane] = sums[lane];
+    __syncwarp();
+    if (lane == 0) {
+        if (it < kMaxIcpIters) {
+            st->ncorr[it] = (int32_t)sums[kIcpVals - 1];
+            st->chol_ok[it] = ok ? 1 : 0;
+        }
+        st->iter = it + 1;
+    }
+}
+
 // MODE 0: one ICP iteration (F, T from the state; the last block updates the pose).
 // MODE 1: association + reduction at the given F, T; the last block writes the sums.
 template <bool PRECISE, int MODE>
@@ -273,15 +366,17 @@ __global__ void __launch_bounds__(kIcpBlock) icp_kernel(const float4* __restrict
             acc.add_pair(k, __ldcg(part_hi + bidx * kIcpVals + k), PRECISE ? __ldcg(part_lo + bidx * kIcpVals + k) : 0.f);
     }
     block_reduce<PRECISE>(acc, sh_hi, sh_lo, red_hi, red_lo);
-    if (threadIdx.x != 0) return;
-    st->ticket = 0u;
-
+    if (threadIdx.x >= 32) return;
+    if (threadIdx.x == 0) st->ticket = 0u;
     if (MODE == 1) {
-        for (int k = 0; k < kIcpVals; ++k) sums_out[k] = PRECISE ? red_hi[k] + red_lo[k] : red_hi[k];
+        if (threadIdx.x < kIcpVals) sums_out[threadIdx.x] = PRECISE ? red_hi[threadIdx.x] + red_lo[threadIdx.x] : red_hi[threadIdx.x];
         return;
     }
-
-    finish_iteration<PRECISE>(st, prm, red_hi, red_lo);
+    if (PRECISE) {
+        if (threadIdx.x == 0) finish_iteration<true>(st, prm, red_hi, red_lo);
+    } else {
+        finish_iteration_warp(st, prm, red_hi);
+    }
 }
 
 // ---- reference summation order ----------------------------------------------------
@@ -290,12 +385,12 @@ __global__ void __launch_bounds__(kIcpBlock) icp_kernel(const float4* __restrict
 // host then adds the 4800 block sums one after another in block order (:369-372).  Here
 // one warp owns a 64-pixel group: lane t holds pixel t and adds pixel t + 32 (the s = 32
 // step), then shuffles down by 16, 8, 4, 2, 1 -- the same additions on the same operands,
-// so each group sum is bit-identical to the reference's.  The last CTA then adds the
+// so each group sum is bit-identical to the reference's.  The reduce pass then adds the
 // group sums in group order.  Groups without a correspondence sum to +0 in every term,
 // and adding +0 to a running sum that starts at +0 never changes it, so those groups are
-// skipped without changing a bit.
+// skipped without changing a bit.  Two launches: a group pass over all SMs and a
+// one-CTA reduce-and-solve pass.
 constexpr int kExactWarps = 8;
-constexpr int kExactChunk = 128;
 
 __device__ __forceinline__ void add_terms(float (&v)[kIcpVals], const float (&a)[6], float b)
 {
@@ -308,17 +403,15 @@ __device__ __forceinline__ void add_terms(float (&v)[kIcpVals], const float (&a)
     v[kIcpVals - 1] = v[kIcpVals - 1] + 1.f;
 }
 
+// Group pass: one warp per 64-pixel group writes the group's 28 sums (27 terms and
+// the correspondence count) and whether the group has a correspondence.
 template <int MODE>
-__global__ void __launch_bounds__(kExactWarps * 32) icp_exact_kernel(
+__global__ void __launch_bounds__(kExactWarps * 32, 4) icp_group_kernel(
     const float4* __restrict__ vmap, const float4* __restrict__ nmap, const float4* __restrict__ pv,
-    const float4* __restrict__ pn, Camera cam, IcpParams prm, State* st, const float* Fsrc, const float* Tsrc,
-    float* partials, int* list, int ngroups, float* sums_out, int32_t* pair)
+    const float4* __restrict__ pn, Camera cam, IcpParams prm, const float* Fsrc, const float* Tsrc,
+    float* __restrict__ partials, int* __restrict__ flags, int ngroups, int32_t* __restrict__ pair)
 {
     __shared__ float sF[16], sT[16];
-    __shared__ float chunk[kExactChunk * kIcpVals];
-    __shared__ int warp_count[kExactWarps];
-    __shared__ int is_last, list_len;
-    __shared__ float red[kIcpVals];
     if (threadIdx.x < 16) {
         sF[threadIdx.x] = Fsrc[threadIdx.x];
         sT[threadIdx.x] = Tsrc[threadIdx.x];
@@ -339,9 +432,7 @@ __global__ void __launch_bounds__(kExactWarps * 32) icp_exact_kernel(
             if (MODE == 1 && pair) pair[i] = ok ? j : -1;
             if (!ok) continue;
             if (half == 0) {
-#pragma unroll
-                for (int k = 0; k < kIcpVals; ++k) v[k] = 0.f;
-                add_terms(v, a, b);  // v = terms of pixel t (0 + x == x exactly)
+                add_terms(v, a, b);  // v = terms of pixel t (0 + x == x up to the sign of a zero)
             } else {
                 float w[kIcpVals];
 #pragma unroll
@@ -356,64 +447,129 @@ __global__ void __launch_bounds__(kExactWarps * 32) icp_exact_kernel(
 #pragma unroll
             for (int k = 0; k < kIcpVals; ++k) v[k] = v[k] + __shfl_down_sync(0xffffffffu, v[k], off);
         if (lane == 0) {
-            list[grp] = v[kIcpVals - 1] != 0.f ? 1 : 0;
+            flags[grp] = v[kIcpVals - 1] != 0.f ? 1 : 0;
+            float4* dst = reinterpret_cast<float4*>(partials + (size_t)grp * kIcpVals);
 #pragma unroll
-            for (int k = 0; k < kIcpVals; ++k) partials[(size_t)grp * kIcpVals + k] = v[k];
-            __threadfence();
+            for (int q = 0; q < kIcpVals / 4; ++q) dst[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
         }
     }
-    __syncthreads();
-    if (threadIdx.x == 0) is_last = (atomicAdd(&st->ticket, 1u) == gridDim.x - 1);
-    __syncthreads();
-    if (!is_last) return;
-    __threadfence();
+}
 
-    // compact the indices of groups with correspondences, in order, in place
-    if (threadIdx.x == 0) list_len = 0;
-    __syncthreads();
-    for (int base = 0; base < ngroups; base += kExactWarps * 32) {
-        const int g = base + threadIdx.x;
-        const int f = g < ngroups ? __ldcg(list + g) : 0;
-        const unsigned m = __ballot_sync(0xffffffffu, f);
-        if (lane == 0) warp_count[warp] = __popc(m);
-        __syncthreads();
-        int off = list_len;
-        for (int w = 0; w < warp; ++w) off += warp_count[w];
-        const int pos = off + __popc(m & ((1u << lane) - 1u));
-        __syncthreads();  // every thread has read its flag and list_len
-        if (f) list[pos] = g;
-        if (threadIdx.x == 0) {
-            int tot = 0;
-            for (int w = 0; w < kExactWarps; ++w) tot += warp_count[w];
-            list_len += tot;
-        }
-        __syncthreads();
+// Reduce-and-solve pass: one warp.  The group sums are streamed into shared memory in
+// order by the bulk-copy engine (cp.async.bulk, double-buffered chunks, mbarrier
+// completion) while the warp adds them: lane k keeps the running sum of term k and
+// reads each chunk from shared memory through a register prefetch, so the serial part
+// is the FADD chain itself.  Empty groups sum to +0 and are added like the rest (exact).
+// Then the warp solves and updates the pose (MODE 0) or writes the sums (MODE 1).
+constexpr int kChunkGroups = 512;                               // 512 x 112 B = 56 KB
+constexpr unsigned kChunkBytes = kChunkGroups * kIcpVals * 4u;  // multiple of 16
+// bounded waits: a copy that has not landed after this many polls is reported, not awaited
+constexpr long long kMaxPolls = 1LL << 26;
+
+__device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, unsigned bytes, unsigned long long* bar)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_addr(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_addr(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ bool bar_wait(unsigned long long* bar, unsigned parity)
+{
+    for (long long i = 0; i < kMaxPolls; ++i) {
+        unsigned done;
+        asm volatile(
+            "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+            : "=r"(done)
+            : "r"(smem_addr(bar)), "r"(parity)
+            : "memory");
+        if (done) return true;
     }
-    __threadfence_block();
-    // serial sum of the group partials in group order, one lane per term
+    return false;
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(32, 1) icp_solve_kernel(const float* __restrict__ partials, int ngroups, State* st,
+                                                        IcpParams prm, float* sums_out)
+{
+    extern __shared__ float4 smem4[];
+    float* buf = reinterpret_cast<float*>(smem4);  // 2 x kChunkGroups x kIcpVals
+    __shared__ __align__(8) unsigned long long bars[2];
+    __shared__ float red[kIcpVals];
+    const int lane = threadIdx.x;
+    const int nchunks = (ngroups + kChunkGroups - 1) / kChunkGroups;
+    auto chunk_bytes = [&](int c) { return (unsigned)(min(kChunkGroups, ngroups - c * kChunkGroups) * kIcpVals * 4); };
+    if (lane == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&bars[0])) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&bars[1])) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        for (int c = 0; c < 2 && c < nchunks; ++c)
+            bulk_load(buf + c * kChunkGroups * kIcpVals, partials + (size_t)c * kChunkGroups * kIcpVals,
+                      chunk_bytes(c), &bars[c]);
+    }
+    __syncwarp();
     float sum = 0.f;
-    for (int base = 0; base < list_len; base += kExactChunk) {
-        const int cnt = min(kExactChunk, list_len - base);
-        for (int e = threadIdx.x; e < cnt * kIcpVals; e += kExactWarps * 32) {
-            const int row = e / kIcpVals, k = e % kIcpVals;
-            chunk[e] = __ldcg(partials + (size_t)list[base + row] * kIcpVals + k);
+    bool ok = true;
+    for (int c = 0; c < nchunks && ok; ++c) {
+        ok = bar_wait(&bars[c & 1], (c >> 1) & 1);
+        if (!ok) break;
+        const float* b = buf + (c & 1) * kChunkGroups * kIcpVals;
+        const int cnt = min(kChunkGroups, ngroups - c * kChunkGroups);
+        if (lane < kIcpVals) {
+            // prefetch 16 sums into registers, then add them in order
+            int r = 0;
+            for (; r + 16 <= cnt; r += 16) {
+                float v[16];
+#pragma unroll
+                for (int q = 0; q < 16; ++q) v[q] = b[(r + q) * kIcpVals + lane];
+#pragma unroll
+                for (int q = 0; q < 16; ++q) sum = sum + v[q];
+            }
+            for (; r < cnt; ++r) sum = sum + b[r * kIcpVals + lane];
         }
-        __syncthreads();
-        if (warp == 0 && lane < kIcpVals) {
-#pragma unroll 8
-            for (int r = 0; r < cnt; ++r) sum = sum + chunk[r * kIcpVals + lane];
+        __syncwarp();
+        if (lane == 0 && c + 2 < nchunks) {
+            // the warp's reads of this buffer precede the async-proxy write that refills it
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            bulk_load(buf + (c & 1) * kChunkGroups * kIcpVals, partials + (size_t)(c + 2) * kChunkGroups * kIcpVals,
+                      chunk_bytes(c + 2), &bars[c & 1]);
         }
-        __syncthreads();
     }
-    if (warp == 0 && lane < kIcpVals) red[lane] = sum;
-    __syncthreads();
-    if (threadIdx.x != 0) return;
-    st->ticket = 0u;
-    if (MODE == 1) {
-        for (int k = 0; k < kIcpVals; ++k) sums_out[k] = red[k];
+    if (!ok) {
+        // a bulk copy did not complete: report it, give the copies in flight a bounded
+        // wait, and leave the pose as it is
+        if (lane == 0) {
+            st->error = 1;
+            for (int k = 0; k < 2; ++k) bar_wait(&bars[k], 0);
+        }
         return;
     }
-    finish_iteration<false>(st, prm, red, red);
+    if (lane < kIcpVals) red[lane] = sum;
+    __syncwarp();
+    if (MODE == 1) {
+        if (lane < kIcpVals) sums_out[lane] = red[lane];
+        return;
+    }
+    finish_iteration_warp(st, prm, red);
+}
+
+size_t solve_smem_bytes(int /*ngroups*/) { return (size_t)2 * kChunkBytes; }
+
+// the reduce-and-solve warp needs more than the default 48 KB of dynamic shared memory
+void ensure_solve_smem(int ngroups)
+{
+    static int configured[64] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const int need = (int)solve_smem_bytes(ngroups);
+    if (dev < 0 || dev >= 64 || configured[dev] >= need) return;
+    cudaFuncSetAttribute(icp_solve_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, need);
+    cudaFuncSetAttribute(icp_solve_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, need);
+    configured[dev] = need;
 }
 
 // device addresses of State members, computed without dereferencing on the host
@@ -431,6 +587,8 @@ int blocks_for(int H, int W)
 int icp_grid_blocks(int H, int W) { return blocks_for(H, W); }
 
 int icp_groups(int H, int W) { return (H * W + 63) / 64; }
+
+void icp_prepare(int H, int W) { ensure_solve_smem(icp_groups(H, W)); }
 
 size_t icp_scratch_floats(int H, int W)
 {
@@ -452,11 +610,13 @@ void launch_icp_iteration(const float4* vmap, const float4* nmap, const float4* 
                           cudaStream_t s)
 {
     const int blocks = blocks_for(cam.H, cam.W);
-    if (!prm.precise && prm.reference_order)
-        icp_exact_kernel<0><<<exact_blocks(cam.H, cam.W), kExactWarps * 32, 0, s>>>(
-            vmap, nmap, pv, pn, cam, prm, st, state_F(st), state_T(st), partials, list, icp_groups(cam.H, cam.W),
-            nullptr, nullptr);
-    else if (prm.precise)
+    if (!prm.precise && prm.reference_order) {
+        const int ng = icp_groups(cam.H, cam.W);
+        ensure_solve_smem(ng);
+        icp_group_kernel<0><<<exact_blocks(cam.H, cam.W), kExactWarps * 32, 0, s>>>(
+            vmap, nmap, pv, pn, cam, prm, state_F(st), state_T(st), partials, list, ng, nullptr);
+        icp_solve_kernel<0><<<1, 32, solve_smem_bytes(ng), s>>>(partials, ng, st, prm, nullptr);
+    } else if (prm.precise)
         icp_kernel<true, 0><<<blocks, kIcpBlock, 0, s>>>(vmap, nmap, pv, pn, cam, prm, st, state_F(st),
                                                          state_T(st), partials, nullptr, nullptr);
     else
@@ -469,10 +629,13 @@ void launch_icp_associate(const float4* vmap, const float4* nmap, const float4* 
                           float* partials, int* list, float* sums_out, int32_t* pair, cudaStream_t s)
 {
     const int blocks = blocks_for(cam.H, cam.W);
-    if (!prm.precise && prm.reference_order)
-        icp_exact_kernel<1><<<exact_blocks(cam.H, cam.W), kExactWarps * 32, 0, s>>>(
-            vmap, nmap, pv, pn, cam, prm, st, F, T, partials, list, icp_groups(cam.H, cam.W), sums_out, pair);
-    else if (prm.precise)
+    if (!prm.precise && prm.reference_order) {
+        const int ng = icp_groups(cam.H, cam.W);
+        ensure_solve_smem(ng);
+        icp_group_kernel<1><<<exact_blocks(cam.H, cam.W), kExactWarps * 32, 0, s>>>(vmap, nmap, pv, pn, cam, prm, F,
+                                                                                    T, partials, list, ng, pair);
+        icp_solve_kernel<1><<<1, 32, solve_smem_bytes(ng), s>>>(partials, ng, st, prm, sums_out);
+    } else if (prm.precise)
         icp_kernel<true, 1><<<blocks, kIcpBlock, 0, s>>>(vmap, nmap, pv, pn, cam, prm, st, F, T, partials, sums_out,
                                                          pair);
     else

@@ -29,6 +29,9 @@ int icp_grid_blocks(int H, int W);
 // 64-pixel groups of the reference-order reduction, and the scratch (floats) both
 // reductions need; list must hold icp_groups() ints
 int icp_groups(int H, int W);
+// once per device and image size, outside any stream capture: raises the dynamic
+// shared-memory limit of the reduce-and-solve kernel
+void icp_prepare(int H, int W);
 size_t icp_scratch_floats(int H, int W);
 void launch_icp_iteration(const float4* vmap, const float4* nmap, const float4* pv, const float4* pn,
                           const Camera& cam, const IcpParams& prm, State* st, float* partials, int* list,

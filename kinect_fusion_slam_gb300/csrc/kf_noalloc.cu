@@ -18,7 +18,7 @@
 // from zero, and calls that overlap on the GPU (different streams at once) race on it.
 #include <mutex>
 
-#include "../../include/kinfu_gb300.h"
+#include "kinfu_gb300.h"
 #include "kf_kernels.h"
 
 namespace {
@@ -71,6 +71,7 @@ cudaError_t scratch_base(unsigned char** out)
         e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess) return e;
         g_base[dev] = static_cast<unsigned char*>(p);
+        kf::icp_prepare(480, 640);  // shared-memory limit of the reduce pass, sized for the largest image
     }
     *out = g_base[dev];
     return cudaSuccess;

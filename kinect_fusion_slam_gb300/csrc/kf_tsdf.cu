@@ -18,12 +18,12 @@ namespace {
 struct VolF32 {
     float* t;
     float* w;
-    __device__ __forceinline__ void load(size_t i, float& tv, float& wv) const
+    __device__ __forceinline__ void load(int i, float& tv, float& wv) const
     {
         tv = t[i];
         wv = w[i];
     }
-    __device__ __forceinline__ void store(size_t i, float tv, float wv) const
+    __device__ __forceinline__ void store(int i, float tv, float wv) const
     {
         t[i] = tv;
         w[i] = wv;
@@ -32,26 +32,23 @@ struct VolF32 {
 
 struct VolF16 {
     __half2* p;
-    __device__ __forceinline__ void load(size_t i, float& tv, float& wv) const
+    __device__ __forceinline__ void load(int i, float& tv, float& wv) const
     {
         const float2 v = __half22float2(p[i]);
         tv = v.x;
         wv = v.y;
     }
-    __device__ __forceinline__ void store(size_t i, float tv, float wv) const { p[i] = __floats2half2_rn(tv, wv); }
+    __device__ __forceinline__ void store(int i, float tv, float wv) const { p[i] = __floats2half2_rn(tv, wv); }
 };
 
 struct ViewF32 {
     const float* t;
-    __device__ __forceinline__ float value(size_t i) const { return __ldg(t + i); }
+    __device__ __forceinline__ float value(int i) const { return __ldg(t + i); }
 };
 
 struct ViewF16 {
     const __half2* p;
-    __device__ __forceinline__ float value(size_t i) const
-    {
-        return __half2float(__low2half(__ldg(p + i)));
-    }
+    __device__ __forceinline__ float value(int i) const { return __half2float(__low2half(__ldg(p + i))); }
 };
 
 // Per pixel (u, v) (1-based): the quantities of projective_tsdf.cu:39-95 that depend
@@ -124,13 +121,54 @@ __global__ void __launch_bounds__(kIntTx* kIntTy) integrate_kernel(Vol vol, cons
     const float tdx = vcx - tx, tdy = vcy - ty;
     const float f0 = ax * tdx + ay * tdy;
     const float m0 = tdx * tdx + tdy * tdy;
+    {
+        // Chunk cull.  The chunk's voxels lie on a segment along z.  The in-front value
+        // front(z) = f0 + az (vcz - tz) and lz(z) are affine in the voxel centre vcz
+        // (monotone in z), and while lz > 50 mm on the whole segment the projection
+        // q(z) = (fx lx + cx lz) / lz is monotone too, so its values at the two ends bound
+        // every voxel's.  The margins (1e-2 mm + 1e-5 relative on front, 1 pixel on q)
+        // exceed the float error of any single voxel's evaluation by orders of magnitude,
+        // so a culled chunk holds no voxel the per-voxel tests below would accept.
+        float fr[2], lzv[2], qu[2], qv[2];
+#pragma unroll
+        for (int e = 0; e < 2; ++e) {
+            const float vcz = centre(e == 0 ? z0 : z1 - 1, g.sz, g.vd);
+            fr[e] = f0 + az * (vcz - tz);
+            const float lx = (a0 + ti[2] * vcz) + ti[3];
+            const float ly = (a1 + ti[6] * vcz) + ti[7];
+            lzv[e] = (a2 + ti[10] * vcz) + ti[11];
+            qu[e] = (fx * lx + cx * lzv[e]) / lzv[e];
+            qv[e] = (fy * ly + cy * lzv[e]) / lzv[e];
+        }
+        const float fm = 1e-2f + 1e-5f * (fabsf(f0) + fabsf(fr[0]) + fabsf(fr[1]));
+        bool cull = fr[0] < -fm && fr[1] < -fm;
+        if (!cull && lzv[0] > 50.f && lzv[1] > 50.f) {
+            const float lo = 0.5f - 1.f, hu = (float)W + 1.5f, hv = (float)H + 1.5f;
+            cull = (qu[0] < lo && qu[1] < lo) || (qu[0] > hu && qu[1] > hu) || (qv[0] < lo && qv[1] < lo) ||
+                   (qv[0] > hv && qv[1] > hv);
+        }
+        if (cull) return;
+    }
     const long long rbase = ((long long)x * g.dy + y) * g.dz;
-    const size_t zstride = (size_t)g.dx * g.dy;
-    size_t lin = ((size_t)z0 * g.dy + y) * g.dx + x;
+    // the reference's guard compares the thread index with the voxel count in float, so
+    // the last z-fastest indices are never integrated; only the last columns get there
+    const bool may_skip = rbase + z1 > skip_from;
+    const int zstride = g.dx * g.dy;  // < 2^31 voxels (checked at kf_create)
+    int lin = (z0 * g.dy + y) * g.dx + x;
+    // a voxel projects to a pixel of the image iff q = px/pz lies in [0.5, W + 0.5) (and
+    // likewise for v); q_approx = px * rcp.approx(pz) is within 2^-21 |q| of the IEEE
+    // quotient, so a voxel whose q_approx is outside the range widened by that bound is
+    // outside exactly and needs neither division (NaN compares false and falls through)
+    const float ulo = 0.5f - 1e-3f, uhi = (float)W + 0.5f + 1e-3f * (float)W;
+    const float vlo = 0.5f - 1e-3f, vhi = (float)H + 0.5f + 1e-3f * (float)H;
     for (int z = z0; z < z1; ++z, lin += zstride) {
-        // the reference's guard compares the thread index with the voxel count in float
-        if (rbase + z >= skip_from) continue;
+        if (may_skip && rbase + z >= skip_from) continue;
         const float vcz = centre(z, g.sz, g.vd);
+        // the reference's tests are independent rejections (all must pass), so the
+        // cheapest runs first: the in-front test (:57-73) needs no projection
+        const float tdz = vcz - tz;
+        const float front = f0 + az * tdz;
+        if (!(front > 0)) continue;
         const float lx = (a0 + ti[2] * vcz) + ti[3];
         const float ly = (a1 + ti[6] * vcz) + ti[7];
         const float lz = (a2 + ti[10] * vcz) + ti[11];
@@ -139,14 +177,15 @@ __global__ void __launch_bounds__(kIntTx* kIntTy) integrate_kernel(Vol vol, cons
         // either way
         const float px = fx * lx + cx * lz;
         const float py = fy * ly + cy * lz;
+        float r;
+        asm("rcp.approx.f32 %0, %1;" : "=f"(r) : "f"(lz));
+        const float qu = px * r, qv = py * r;
+        if (qu < ulo || qu > uhi || qv < vlo || qv > vhi) continue;
         const int u = (int)roundf(px / lz);
         const int v = (int)roundf(py / lz);
         if (u < 1 || u > W || v < 1 || v > H) continue;
         const float2 e = __ldg(tab + (v - 1) * W + (u - 1));
         if (isnan(e.x)) continue;
-        const float tdz = vcz - tz;
-        const float front = f0 + az * tdz;
-        if (!(front > 0)) continue;
         const float tm = sqrtf(m0 + tdz * tdz);
         const float frk = e.x - e.y * tm;
         const bool ahead = frk > 0 && frk <= g.sdf_max;
@@ -244,7 +283,8 @@ __device__ __forceinline__ void trace(const View& vol, float X, float Y, float D
     if (ix == L + 1) ix = ix - 1;
     if (iy == Wd + 1) iy = iy - 1;
     if (iz == Hz + 1) iz = iz - 1;
-    float tvx, tvy, tvz, sx, sy, sz;
+    float tvx, tvy, tvz;
+    int sx, sy, sz;  // the reference steps by a float +-1; integer steps give the same indices
     if (dir.x >= 0) {
         tvx = (float)(ix) / L;
         sx = 1;
@@ -270,100 +310,169 @@ __device__ __forceinline__ void trace(const View& vol, float X, float Y, float D
     float3 tm = make_float3(tmin + ((vmax.x - s.x) / dir.x), tmin + ((vmax.y - s.y) / dir.y),
                             tmin + ((vmax.z - s.z) / dir.z));
     const float3 td = make_float3(vd / fabsf(dir.x), vd / fabsf(dir.y), vd / fabsf(dir.z));
-    const float fL = (float)L, fW = (float)Wd, fH = (float)Hz;
-    const size_t ys = (size_t)L, zs = (size_t)L * Wd;
-    auto lin = [&](int a, int b, int c) -> size_t { return (size_t)c * zs + (size_t)b * ys + (size_t)a; };
+    const int ys = L, zs = L * Wd;  // < 2^31 voxels (checked at kf_create)
+    const int dlx = sx, dly = sy * ys, dlz = sz * zs;
+    auto lin = [&](int a, int b, int c) -> int { return c * zs + b * ys + a; };
+    int li = lin(ix - 1, iy - 1, iz - 1);
 
-    float prev = 0.0f;
-    // every iteration moves one index one step in a fixed direction, so the walk ends
-    // within L + Wd + Hz iterations; the bound only makes that explicit
-    for (int guard = 0; guard < L + Wd + Hz + 4; ++guard) {
-        if (!(ix < (fL - 1) && ix > 0 && iy < (fW - 1) && iy > 0 && iz < (fH - 1) && iz > 0)) break;
-        const float cur = vol.value(lin(ix - 1, iy - 1, iz - 1));
-        if (isnan(cur) && prev < 0.f) break;
-        if (cur < 0.f && isnan(prev)) break;
-        if (cur > 0.f && prev < 0.f) break;
-        if (cur < 0.f && prev > 0.f) {
-            const int xn = (ix - 1) - 1, xp = (ix - 1) + 1;
-            const int yn = (iy - 1) - 1, yp = (iy - 1) + 1;
-            const int zn = (iz - 1) - 1, zp = (iz - 1) + 1;
-            // :233-282; recorded indices are checked against the stepped axis' extent
-            if (xn >= L || xn < 0 || xp >= L || xp < 0) break;
-            if ((XY - 1) >= L || (XY - 1) < 0 || (XZ - 1) >= L || (XZ - 1) < 0) break;
-            if (yn >= Wd || yn < 0 || yp >= Wd || yp < 0) break;
-            if ((YX - 1) >= Wd || (YX - 1) < 0 || (YZ - 1) >= Wd || (YZ - 1) < 0) break;
-            if (zn >= Hz || zn < 0 || zp >= Hz || zp < 0) break;
-            if ((ZX - 1) >= Hz || (ZX - 1) < 0 || (ZY - 1) >= Hz || (ZY - 1) < 0) break;
-            // the recorded indices are in range for their own axes (they were loop
-            // positions), so every neighbour below lies inside the grid
-            const float v_xnp = vol.value(lin(xn, XY - 1, XZ - 1));
-            const float v_xpp = vol.value(lin(xp, XY - 1, XZ - 1));
-            const float v_ynp = vol.value(lin(YX - 1, yn, YZ - 1));
-            const float v_ypp = vol.value(lin(YX - 1, yp, YZ - 1));
-            const float v_znp = vol.value(lin(ZX - 1, ZY - 1, zn));
-            const float v_zpp = vol.value(lin(ZX - 1, ZY - 1, zp));
-            if (isnan(v_xnp) || isnan(v_xpp) || isnan(v_ynp) || isnan(v_ypp) || isnan(v_znp) || isnan(v_zpp) ||
-                isnan(cur))
-                break;
-            const float v_xnn = vol.value(lin(ix - 2, iy - 1, iz - 1));
-            const float v_xpn = vol.value(lin(ix, iy - 1, iz - 1));
-            const float v_ynn = vol.value(lin(ix - 1, iy - 2, iz - 1));
-            const float v_ypn = vol.value(lin(ix - 1, iy, iz - 1));
-            const float v_znn = vol.value(lin(ix - 1, iy - 1, iz - 2));
-            const float v_zpn = vol.value(lin(ix - 1, iy - 1, iz));
-            if (isnan(v_xnn) || isnan(v_xpn) || isnan(v_ynn) || isnan(v_ypn) || isnan(v_znn) || isnan(v_zpn)) break;
-            float3 sp;
-            // per-axis linear zero crossing (:318-349)
-            if (dir.x > 0)
-                sp.x = centre(xn, g.sx, vd) + vd * (fabsf(v_xnp) / (fabsf(v_xnp - cur)));
-            else
-                sp.x = centre(xp, g.sx, vd) - vd * (fabsf(v_xpp) / (fabsf(v_xpp - cur)));
-            if (dir.y > 0)
-                sp.y = centre(yn, g.sy, vd) + vd * (fabsf(v_ynp) / (fabsf(v_ynp - cur)));
-            else
-                sp.y = centre(yp, g.sy, vd) - vd * (fabsf(v_ypp) / (fabsf(v_ypp - cur)));
-            if (dir.z > 0)
-                sp.z = centre(zn, g.sz, vd) + vd * (fabsf(v_znp) / (fabsf(v_znp - cur)));
-            else
-                sp.z = centre(zp, g.sz, vd) - vd * (fabsf(v_zpp) / (fabsf(v_zpp - cur)));
-            const float3 nr = make_float3((v_xpn - v_xnn) / 2.0f, (v_ypn - v_ynn) / 2.0f, (v_zpn - v_znn) / 2.0f);
-            const float3 va = normalized(make_float3(cam.x - sp.x, cam.y - sp.y, cam.z - sp.z));
-            float3 vb = normalized(nr);
-            const float ct = va.x * vb.x + va.y * vb.y + va.z * vb.z;
-            if (ct < c_flip) vb = make_float3(-vb.x, -vb.y, -vb.z);
-            op = make_float4(sp.x, sp.y, sp.z, 0.f);
-            on = make_float4(vb.x, vb.y, vb.z, 0.f);
-            oh = ((ix - 1) * Wd + (iy - 1)) * Hz + (iz - 1);
-            return;
-        }
-        prev = cur;
-        // Amanatides-Woo step (:384-417)
-        if (tm.x < tm.y) {
-            if (tm.x < tm.z) {
-                ix = ix + sx;
-                XY = iy;
-                XZ = iz;
-                tm.x = tm.x + td.x;
+    // 0 < i < n-1 as one unsigned compare per axis
+    auto inside_grid = [&](int a, int b, int c) {
+        return (unsigned)(a - 1) < (unsigned)(L - 2) && (unsigned)(b - 1) < (unsigned)(Wd - 2) &&
+               (unsigned)(c - 1) < (unsigned)(Hz - 2);
+    };
+    // The stepping never depends on the loaded values, only the termination does, so a
+    // lead walker with the same arithmetic runs kAhead steps in front and issues the
+    // loads early into a register ring; the trailing walk consumes them in order.  The
+    // lead loads only voxels inside the loop bounds.
+    constexpr int kAhead = 4;
+    int ax = ix, ay = iy, az = iz, ali = li;
+    float3 atm = tm;
+    auto lead_step = [&]() {
+        if (atm.x < atm.y) {
+            if (atm.x < atm.z) {
+                ax += sx;
+                ali += dlx;
+                atm.x = atm.x + td.x;
             } else {
-                iz = iz + sz;
-                ZX = ix;
-                ZY = iy;
-                tm.z = tm.z + td.z;
+                az += sz;
+                ali += dlz;
+                atm.z = atm.z + td.z;
             }
         } else {
-            if (tm.y < tm.z) {
-                iy = iy + sy;
-                YX = ix;
-                YZ = iz;
-                tm.y = tm.y + td.y;
+            if (atm.y < atm.z) {
+                ay += sy;
+                ali += dly;
+                atm.y = atm.y + td.y;
             } else {
-                iz = iz + sz;
-                ZX = ix;
-                ZY = iy;
-                tm.z = tm.z + td.z;
+                az += sz;
+                ali += dlz;
+                atm.z = atm.z + td.z;
+            }
+        }
+    };
+    float ring[kAhead];
+#pragma unroll
+    for (int k = 0; k < kAhead; ++k) {
+        ring[k] = inside_grid(ax, ay, az) ? vol.value(ali) : 0.f;
+        lead_step();
+    }
+
+    float prev = 0.0f;
+    float crossing = 0.f;  // the negative value met right after a positive one, or 0
+    bool done = false;
+    // every iteration moves one index one step in a fixed direction, so the walk ends
+    // within L + Wd + Hz steps; the bound only makes that explicit
+    for (int guard = 0; !done && guard < L + Wd + Hz + 4; guard += kAhead) {
+#pragma unroll
+        for (int k = 0; k < kAhead; ++k) {
+            if (!inside_grid(ix, iy, iz)) {
+                done = true;
+                break;
+            }
+            const float cur = ring[k];
+            ring[k] = inside_grid(ax, ay, az) ? vol.value(ali) : 0.f;
+            lead_step();
+            // the reference's four tests (:207-222) are mutually exclusive in prev
+            if (prev < 0.f) {
+                if (!(cur <= 0.f)) {  // NaN or back face
+                    done = true;
+                    break;
+                }
+            } else if (isnan(prev)) {
+                if (cur < 0.f) {
+                    done = true;
+                    break;
+                }
+            } else if (prev > 0.f && cur < 0.f) {
+                // zero crossing: leave the walk with the state as it is and resolve it
+                // below, where the warp's lanes have reconverged
+                crossing = cur;
+                done = true;
+                break;
+            }
+            prev = cur;
+            // Amanatides-Woo step (:384-417)
+            if (tm.x < tm.y) {
+                if (tm.x < tm.z) {
+                    ix += sx;
+                    li += dlx;
+                    XY = iy;
+                    XZ = iz;
+                    tm.x = tm.x + td.x;
+                } else {
+                    iz += sz;
+                    li += dlz;
+                    ZX = ix;
+                    ZY = iy;
+                    tm.z = tm.z + td.z;
+                }
+            } else {
+                if (tm.y < tm.z) {
+                    iy += sy;
+                    li += dly;
+                    YX = ix;
+                    YZ = iz;
+                    tm.y = tm.y + td.y;
+                } else {
+                    iz += sz;
+                    li += dlz;
+                    ZX = ix;
+                    ZY = iy;
+                    tm.z = tm.z + td.z;
+                }
             }
         }
     }
+    if (!(crossing < 0.f)) return;
+    const float cur = crossing;
+    const int xn = (ix - 1) - 1, xp = (ix - 1) + 1;
+    const int yn = (iy - 1) - 1, yp = (iy - 1) + 1;
+    const int zn = (iz - 1) - 1, zp = (iz - 1) + 1;
+    // :233-282; recorded indices are checked against the stepped axis' extent
+    if (xn >= L || xn < 0 || xp >= L || xp < 0) return;
+    if ((XY - 1) >= L || (XY - 1) < 0 || (XZ - 1) >= L || (XZ - 1) < 0) return;
+    if (yn >= Wd || yn < 0 || yp >= Wd || yp < 0) return;
+    if ((YX - 1) >= Wd || (YX - 1) < 0 || (YZ - 1) >= Wd || (YZ - 1) < 0) return;
+    if (zn >= Hz || zn < 0 || zp >= Hz || zp < 0) return;
+    if ((ZX - 1) >= Hz || (ZX - 1) < 0 || (ZY - 1) >= Hz || (ZY - 1) < 0) return;
+    // the recorded indices are in range for their own axes (they were loop positions),
+    // so every neighbour below lies inside the grid
+    const float v_xnp = vol.value(lin(xn, XY - 1, XZ - 1));
+    const float v_xpp = vol.value(lin(xp, XY - 1, XZ - 1));
+    const float v_ynp = vol.value(lin(YX - 1, yn, YZ - 1));
+    const float v_ypp = vol.value(lin(YX - 1, yp, YZ - 1));
+    const float v_znp = vol.value(lin(ZX - 1, ZY - 1, zn));
+    const float v_zpp = vol.value(lin(ZX - 1, ZY - 1, zp));
+    const float v_xnn = vol.value(li - 1);
+    const float v_xpn = vol.value(li + 1);
+    const float v_ynn = vol.value(li - ys);
+    const float v_ypn = vol.value(li + ys);
+    const float v_znn = vol.value(li - zs);
+    const float v_zpn = vol.value(li + zs);
+    if (isnan(v_xnp) || isnan(v_xpp) || isnan(v_ynp) || isnan(v_ypp) || isnan(v_znp) || isnan(v_zpp)) return;
+    if (isnan(v_xnn) || isnan(v_xpn) || isnan(v_ynn) || isnan(v_ypn) || isnan(v_znn) || isnan(v_zpn)) return;
+    float3 sp;
+    // per-axis linear zero crossing (:318-349)
+    if (dir.x > 0)
+        sp.x = centre(xn, g.sx, vd) + vd * (fabsf(v_xnp) / (fabsf(v_xnp - cur)));
+    else
+        sp.x = centre(xp, g.sx, vd) - vd * (fabsf(v_xpp) / (fabsf(v_xpp - cur)));
+    if (dir.y > 0)
+        sp.y = centre(yn, g.sy, vd) + vd * (fabsf(v_ynp) / (fabsf(v_ynp - cur)));
+    else
+        sp.y = centre(yp, g.sy, vd) - vd * (fabsf(v_ypp) / (fabsf(v_ypp - cur)));
+    if (dir.z > 0)
+        sp.z = centre(zn, g.sz, vd) + vd * (fabsf(v_znp) / (fabsf(v_znp - cur)));
+    else
+        sp.z = centre(zp, g.sz, vd) - vd * (fabsf(v_zpp) / (fabsf(v_zpp - cur)));
+    const float3 nr = make_float3((v_xpn - v_xnn) / 2.0f, (v_ypn - v_ynn) / 2.0f, (v_zpn - v_znn) / 2.0f);
+    const float3 va = normalized(make_float3(cam.x - sp.x, cam.y - sp.y, cam.z - sp.z));
+    float3 vb = normalized(nr);
+    const float ct = va.x * vb.x + va.y * vb.y + va.z * vb.z;
+    if (ct < c_flip) vb = make_float3(-vb.x, -vb.y, -vb.z);
+    op = make_float4(sp.x, sp.y, sp.z, 0.f);
+    on = make_float4(vb.x, vb.y, vb.z, 0.f);
+    oh = ((ix - 1) * Wd + (iy - 1)) * Hz + (iz - 1);
 }
 
 constexpr int kRayTile = 16;

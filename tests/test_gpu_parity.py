@@ -108,6 +108,38 @@ def test_raycast(oracle, small_seq):
         assert np.all(pred_g[:, ~m] == 0)
 
 
+def test_integration_raycast_c1(oracle):
+    """The bench's size: 640x480 into 360x360x300 @ 10 mm, three frames at ground-truth
+    poses plus one at a perturbed pose; every integrated voxel, weight and hit index bit
+    for bit."""
+    from kinect_fusion_slam_gb300 import scene
+
+    seq = scene.sequence("c1", frames=4)
+    depths = seq.depths(4)
+    gs = grid_spec(seq.cfg.grid)
+    h = make_handle(seq)
+    K = seq.K
+    Ki = oracle.inv3(K)
+    to = np.full(gs.nvox, np.nan, np.float32)
+    wo = np.full(gs.nvox, np.nan, np.float32)
+    rng = np.random.default_rng(5)
+    for n, k in enumerate(range(4)):
+        T = seq.poses[k].astype(np.float32)
+        if k == 3:
+            T[:3, 3] += rng.normal(0, 20, 3).astype(np.float32)
+        d = oracle.depth_ingest(depths[k])
+        h.set_pose(T)
+        h.set_depth_f32(d)
+        h.projective_tsdf(first=(n == 0))
+        oracle.integrate(gs, d, K, Ki, T, oracle.inv4(T), to, wo, first=(n == 0))
+        hit_g = h.ray_casting()
+        pred_o, hit_o = oracle.raycast(gs, d, Ki, T, to)
+        assert np.array_equal(hit_g, hit_o), f"frame {k}: {int((hit_g != hit_o).sum())} hits differ"
+    tg, wg = h.volume()
+    assert_volume_parity(tg, wg, to, wo)
+    assert int((~np.isnan(wo)).sum()) > 100000 and int((hit_o >= 0).sum()) > 100000
+
+
 def test_flip_threshold(oracle, small_seq):
     """The ray-cast normal flip uses a float threshold the device derives from its own
     double acos; it must equal the threshold of the oracle's libm acos."""
