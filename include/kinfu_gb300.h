@@ -101,7 +101,8 @@ kf_status kf_get_intrinsics(const kf_handle* h, float K[9]);
 /* extrinsic_matrix (kinfu_pipeline.h:18): 4x4 row-major camera-to-world, mm */
 kf_status kf_set_pose(kf_handle* h, const float T[16]);
 kf_status kf_get_pose(kf_handle* h, float T[16]);
-/* resets the volume to NaN and the pose to identity */
+/* resets the volume to NaN and the pose to identity; asynchronous on the handle's
+ * stream, like the frame calls (the next frame call is kf_initial_processing) */
 kf_status kf_reset(kf_handle* h);
 
 /* ---- frame loop (KinfuPipeline) --------------------------------------------------

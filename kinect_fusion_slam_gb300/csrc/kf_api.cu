@@ -41,6 +41,7 @@ struct kf_handle {
     State* d_state = nullptr;
     float* d_partials = nullptr;
     int* d_groups = nullptr;  // ICP group flags / compacted group list
+    unsigned* d_tiles = nullptr;  // ray-cast tile counter
     float* d_mats = nullptr;  // F, T (debug association input) + sums output
     float* d_spatial = nullptr;
 
@@ -197,9 +198,11 @@ void enq_integrate(kf_handle* h, bool first)
 void enq_raycast(kf_handle* h, int32_t* hit)
 {
     if (h->d_vol16)
-        launch_raycast_f16(h->d_vol16, h->d_depth, h->d_pv, h->d_pn, hit, h->cam, h->grid, h->d_state, h->stream);
+        launch_raycast_f16(h->d_vol16, h->d_depth, h->d_pv, h->d_pn, hit, h->cam, h->grid, h->d_state, h->d_tiles,
+                           h->stream);
     else
-        launch_raycast_f32(h->d_tsdf, h->d_depth, h->d_pv, h->d_pn, hit, h->cam, h->grid, h->d_state, h->stream);
+        launch_raycast_f32(h->d_tsdf, h->d_depth, h->d_pv, h->d_pn, hit, h->cam, h->grid, h->d_state, h->d_tiles,
+                           h->stream);
 }
 
 // stage timing event k; inside a stream capture the record must be an external
@@ -325,6 +328,8 @@ kf_status allocate(kf_handle* h)
     KF_TRY(dalloc(h, &h->d_state, 1));
     KF_TRY(dalloc(h, &h->d_partials, icp_scratch_floats(h->cam.H, h->cam.W)));
     KF_TRY(dalloc(h, &h->d_groups, (size_t)icp_groups(h->cam.H, h->cam.W)));
+    KF_TRY(dalloc(h, &h->d_tiles, 2));
+    KF_CUDA(h, cudaMemset(h->d_tiles, 0, 2 * sizeof(unsigned)));
     KF_TRY(dalloc(h, &h->d_mats, 64));
     KF_TRY(dalloc(h, &h->d_spatial, 15 * 15));
     if (h->cfg.tsdf_storage == KF_TSDF_F16) {
@@ -339,7 +344,8 @@ kf_status allocate(kf_handle* h)
     return KF_OK;
 }
 
-kf_status reset_state(kf_handle* h)
+// volume to NaN, images to "no data"; stream-ordered, no host synchronisation
+kf_status enqueue_clear(kf_handle* h)
 {
     const size_t HW = (size_t)h->cam.H * h->cam.W;
     if (h->d_vol16)
@@ -355,6 +361,13 @@ kf_status reset_state(kf_handle* h)
     KF_CUDA(h, cudaMemsetAsync(h->d_pv, 0, sizeof(float4) * HW, h->stream));
     KF_CUDA(h, cudaMemsetAsync(h->d_pn, 0, sizeof(float4) * HW, h->stream));
     KF_CUDA(h, cudaMemsetAsync(h->d_hit, 0xff, sizeof(int32_t) * HW, h->stream));
+    return KF_OK;
+}
+
+// first initialisation at kf_create: clear, identity pose, calibrated c_flip
+kf_status reset_state(kf_handle* h)
+{
+    KF_TRY(enqueue_clear(h));
     std::memset(h->h_state, 0, sizeof(State));
     for (int k = 0; k < 16; ++k) {
         h->h_state->T[k] = (k % 5 == 0) ? 1.f : 0.f;
@@ -372,7 +385,7 @@ void free_all(kf_handle* h)
     destroy_graphs(h);
     void* dev[] = {h->d_raw, h->d_depth, h->d_depth_tmp, h->d_vmap, h->d_nmap, h->d_pv, h->d_pn, h->d_hit,
                    h->d_pair, h->d_tab, h->d_tsdf, h->d_weight, h->d_vol16, h->d_state, h->d_partials, h->d_groups,
-                   h->d_mats,
+                   h->d_tiles, h->d_mats,
                    h->d_spatial};
     for (void* p : dev)
         if (p) cudaFree(p);
@@ -473,7 +486,10 @@ kf_status kf_create(const kf_config* cfg, kf_handle** out)
     if (cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking) != cudaSuccess) s = KF_ERR_CUDA;
     h->stream = h->own_stream;
     if (s == KF_OK) s = allocate(h);
-    if (s == KF_OK) icp_prepare(h->cam.H, h->cam.W);
+    if (s == KF_OK) {
+        icp_prepare(h->cam.H, h->cam.W);
+        raycast_blocks();
+    }
     if (s == KF_OK && cfg->bilateral) s = upload_spatial(h);
     if (s == KF_OK) s = reset_state(h);
     if (s != KF_OK) {
@@ -559,8 +575,10 @@ kf_status kf_get_pose(kf_handle* h, float T[16])
 kf_status kf_reset(kf_handle* h)
 {
     KF_HANDLE(h);
-    KF_CUDA(h, cudaStreamSynchronize(h->stream));
-    return reset_state(h);
+    KF_TRY(enqueue_clear(h));
+    launch_state_reset(h->d_state, h->stream);
+    KF_CHECK_LAUNCH(h);
+    return KF_OK;
 }
 
 kf_status kf_synchronize(kf_handle* h)
@@ -906,8 +924,10 @@ kf_status kf_get_stage_times(kf_handle* h, float ms[5])
 kf_status kf_kernels_per_frame(kf_handle* h, int* n)
 {
     if (!h || !n) return KF_ERR_INVALID_ARGUMENT;
-    // vertex, [bilateral], ICP iterations, integration prep, integration, ray cast
-    *n = 1 + (h->cfg.bilateral ? 1 : 0) + h->cfg.icp_iterations[0] + 3;
+    // vertex, [bilateral], ICP iterations (associate + reduce, then a one-warp solve in
+    // the reference summation order), integration prep, integration, ray cast
+    const int per_iteration = h->cfg.icp_reduction == KF_REDUCE_REFERENCE_ORDER ? 2 : 1;
+    *n = 1 + (h->cfg.bilateral ? 1 : 0) + per_iteration * h->cfg.icp_iterations[0] + 3;
     return KF_OK;
 }
 

@@ -165,6 +165,21 @@ __global__ void calibrate_kernel(State* st)
     st->c_flip = key_float(hi);
 }
 
+// pose back to identity, ICP bookkeeping and error flag to zero; keeps the calibrated c_flip
+__global__ void state_reset_kernel(State* st)
+{
+    const float c_flip = st->c_flip;
+    __syncthreads();
+    unsigned* w = reinterpret_cast<unsigned*>(st);
+    for (int i = threadIdx.x; i < (int)(sizeof(State) / sizeof(unsigned)); i += blockDim.x) w[i] = 0u;
+    __syncthreads();
+    if (threadIdx.x < 16) {
+        st->T[threadIdx.x] = (threadIdx.x % 5 == 0) ? 1.f : 0.f;
+        st->Td[threadIdx.x] = (threadIdx.x % 5 == 0) ? 1.0 : 0.0;
+    }
+    if (threadIdx.x == 0) st->c_flip = c_flip;
+}
+
 // x-fastest (device) <-> z-fastest (reference) volume order
 __global__ void to_zfast_kernel(const float* __restrict__ src, float* __restrict__ dst, Grid g)
 {
@@ -244,6 +259,8 @@ void launch_bilateral(const float* depth, float* out, const float* spatial, int 
 }
 
 void launch_calibrate(State* st, cudaStream_t s) { calibrate_kernel<<<1, 32, 0, s>>>(st); }
+
+void launch_state_reset(State* st, cudaStream_t s) { state_reset_kernel<<<1, 256, 0, s>>>(st); }
 
 void launch_to_zfast_f32(const float* src, float* dst, const Grid& g, cudaStream_t s)
 {

@@ -13,6 +13,7 @@
 #include <cstddef>
 
 #include "kf_kernels.h"
+#include "kf_launch.cuh"
 
 namespace kf {
 
@@ -218,7 +219,10 @@ __device__ void finish_iteration(State* st, const IcpParams& prm, const float* h
 // is formed column by column -- each entry from the same operands in the same order as
 // cv::Cholesky's row-by-row loop, so every bit is the same -- and each entry of the two
 // 4x4 products is computed by its own lane.  All 32 lanes of the calling warp must call.
-__device__ void finish_iteration_warp(State* st, const IcpParams& prm, const float* sums)
+// T0 and Tprev_inv: the state's T and Tprev_inv, already loaded by the caller (shared
+// memory), so their global-memory latency overlaps the reduction; it: the state's iter
+__device__ void finish_iteration_warp(State* st, const IcpParams& prm, const float* sums, const float* T0,
+                                      const float* Tprev_inv, int it)
 {
     __shared__ float L[36], xb[6], inc[16], Tn[16];
     __shared__ int fail;
@@ -248,7 +252,7 @@ __device__ void finish_iteration_warp(State* st, const IcpParams& prm, const flo
             if (sd < FLT_EPSILON)
                 fail = 1;
             else
-                L[j * 6 + j] = (float)(1. / sqrt(sd));
+                L[j * 6 + j] = rsqrt_pivot(sd);
         }
         __syncwarp();
         if (fail) break;
@@ -277,23 +281,22 @@ __device__ void finish_iteration_warp(State* st, const IcpParams& prm, const flo
     // T <- Inc * T and F <- T_prev^-1 * T, one output entry per lane (kf::mat4's order)
     if (lane < 16) {
         const int r = lane >> 2, c = lane & 3;
-        double a = (double)inc[r * 4 + 0] * st->T[c];
-        a += (double)inc[r * 4 + 1] * st->T[4 + c];
-        a += (double)inc[r * 4 + 2] * st->T[8 + c];
-        a += (double)inc[r * 4 + 3] * st->T[12 + c];
+        double a = (double)inc[r * 4 + 0] * T0[c];
+        a += (double)inc[r * 4 + 1] * T0[4 + c];
+        a += (double)inc[r * 4 + 2] * T0[8 + c];
+        a += (double)inc[r * 4 + 3] * T0[12 + c];
         Tn[lane] = (float)a;
     }
     __syncwarp();
     if (lane < 16) {
         st->T[lane] = Tn[lane];
         const int r = lane >> 2, c = lane & 3;
-        double a = (double)st->Tprev_inv[r * 4 + 0] * Tn[c];
-        a += (double)st->Tprev_inv[r * 4 + 1] * Tn[4 + c];
-        a += (double)st->Tprev_inv[r * 4 + 2] * Tn[8 + c];
-        a += (double)st->Tprev_inv[r * 4 + 3] * Tn[12 + c];
+        double a = (double)Tprev_inv[r * 4 + 0] * Tn[c];
+        a += (double)Tprev_inv[r * 4 + 1] * Tn[4 + c];
+        a += (double)Tprev_inv[r * 4 + 2] * Tn[8 + c];
+        a += (double)Tprev_inv[r * 4 + 3] * Tn[12 + c];
         st->F[lane] = (float)a;
     }
-    const int it = st->iter;
     if (it < kMaxIcpIters && lane < 16) st->Tlog[it][lane] = Tn[lane];
     if (lane < kIcpVals) st->sums[lane] = sums[lane];
     __syncwarp();
@@ -375,7 +378,13 @@ __global__ void __launch_bounds__(kIcpBlock) icp_kernel(const float4* __restrict
     if (PRECISE) {
         if (threadIdx.x == 0) finish_iteration<true>(st, prm, red_hi, red_lo);
     } else {
-        finish_iteration_warp(st, prm, red_hi);
+        __shared__ float sT0[16], sTp[16];
+        if (threadIdx.x < 16) {
+            sT0[threadIdx.x] = st->T[threadIdx.x];
+            sTp[threadIdx.x] = st->Tprev_inv[threadIdx.x];
+        }
+        __syncwarp();
+        finish_iteration_warp(st, prm, red_hi, sT0, sTp, st->iter);
     }
 }
 
@@ -411,6 +420,7 @@ __global__ void __launch_bounds__(kExactWarps * 32, 4) icp_group_kernel(
     const float4* __restrict__ pn, Camera cam, IcpParams prm, const float* Fsrc, const float* Tsrc,
     float* __restrict__ partials, int* __restrict__ flags, int ngroups, int32_t* __restrict__ pair)
 {
+    wait_for_producer();
     __shared__ float sF[16], sT[16];
     if (threadIdx.x < 16) {
         sF[threadIdx.x] = Fsrc[threadIdx.x];
@@ -456,12 +466,19 @@ __global__ void __launch_bounds__(kExactWarps * 32, 4) icp_group_kernel(
 }
 
 // Reduce-and-solve pass: one warp.  The group sums are streamed into shared memory in
-// order by the bulk-copy engine (cp.async.bulk, double-buffered chunks, mbarrier
-// completion) while the warp adds them: lane k keeps the running sum of term k and
-// reads each chunk from shared memory through a register prefetch, so the serial part
-// is the FADD chain itself.  Empty groups sum to +0 and are added like the rest (exact).
-// Then the warp solves and updates the pose (MODE 0) or writes the sums (MODE 1).
+// order by the bulk-copy engine (cp.async.bulk into a ring of kBuffers chunks with
+// mbarrier completion; kBuffers - 1 copies stay in flight) while the warp adds them:
+// lane k keeps the running sum of term k.  The additions run as one software pipeline
+// over batches of kBatch groups -- the next batch's shared-memory loads are issued
+// before the current batch's additions, across chunk boundaries too -- so the serial
+// part is the FADD chain itself.  Empty groups sum to +0 and are added like the rest
+// (exact).  Then the warp solves and updates the pose (MODE 0) or writes the sums
+// (MODE 1).
 constexpr int kChunkGroups = 512;                               // 512 x 112 B = 56 KB
+constexpr int kBuffers = 2;
+constexpr int kBatch = 16;
+constexpr int kBatchesPerChunk = kChunkGroups / kBatch;
+static_assert(kChunkGroups % (2 * kBatch) == 0, "a chunk is an even number of batches");
 constexpr unsigned kChunkBytes = kChunkGroups * kIcpVals * 4u;  // multiple of 16
 // bounded waits: a copy that has not landed after this many polls is reported, not awaited
 constexpr long long kMaxPolls = 1LL << 26;
@@ -496,47 +513,97 @@ template <int MODE>
 __global__ void __launch_bounds__(32, 1) icp_solve_kernel(const float* __restrict__ partials, int ngroups, State* st,
                                                         IcpParams prm, float* sums_out)
 {
+    wait_for_producer();
     extern __shared__ float4 smem4[];
-    float* buf = reinterpret_cast<float*>(smem4);  // 2 x kChunkGroups x kIcpVals
-    __shared__ __align__(8) unsigned long long bars[2];
+    float* buf = reinterpret_cast<float*>(smem4);  // kBuffers x kChunkGroups x kIcpVals
+    __shared__ __align__(8) unsigned long long bars[kBuffers];
     __shared__ float red[kIcpVals];
+    __shared__ float sT0[16], sTp[16];
     const int lane = threadIdx.x;
+    // the pose inputs of the solve, loaded now so their latency hides behind the sums
+    float t0 = 0.f, tp = 0.f;
+    int it = 0;
+    if (MODE == 0) {
+        if (lane < 16) {
+            t0 = st->T[lane];
+            tp = st->Tprev_inv[lane];
+        }
+        it = st->iter;
+    }
     const int nchunks = (ngroups + kChunkGroups - 1) / kChunkGroups;
     auto chunk_bytes = [&](int c) { return (unsigned)(min(kChunkGroups, ngroups - c * kChunkGroups) * kIcpVals * 4); };
     if (lane == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&bars[0])) : "memory");
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&bars[1])) : "memory");
+        for (int k = 0; k < kBuffers; ++k)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&bars[k])) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        for (int c = 0; c < 2 && c < nchunks; ++c)
+        for (int c = 0; c < kBuffers && c < nchunks; ++c)
             bulk_load(buf + c * kChunkGroups * kIcpVals, partials + (size_t)c * kChunkGroups * kIcpVals,
                       chunk_bytes(c), &bars[c]);
     }
     __syncwarp();
+    // lanes 28..31 read term 27's column too (in bounds) and discard it
+    const int term = lane < kIcpVals ? lane : kIcpVals - 1;
+    auto slot_ptr = [&](int c) { return buf + (c % kBuffers) * kChunkGroups * kIcpVals + term; };
     float sum = 0.f;
-    bool ok = true;
-    for (int c = 0; c < nchunks && ok; ++c) {
-        ok = bar_wait(&bars[c & 1], (c >> 1) & 1);
-        if (!ok) break;
-        const float* b = buf + (c & 1) * kChunkGroups * kIcpVals;
-        const int cnt = min(kChunkGroups, ngroups - c * kChunkGroups);
-        if (lane < kIcpVals) {
-            // prefetch 16 sums into registers, then add them in order
-            int r = 0;
-            for (; r + 16 <= cnt; r += 16) {
-                float v[16];
+    bool ok = nchunks == 0 || bar_wait(&bars[0], 0);
+    const int full = ngroups / kChunkGroups;  // chunks of exactly kChunkGroups groups
+    float va[kBatch], vb[kBatch];
+    if (ok && full > 0) {
+        const float* p = slot_ptr(0);
 #pragma unroll
-                for (int q = 0; q < 16; ++q) v[q] = b[(r + q) * kIcpVals + lane];
+        for (int q = 0; q < kBatch; ++q) va[q] = p[q * kIcpVals];
+    }
+    for (int c = 0; c < full && ok; ++c) {
+        // batches 0..kBatchesPerChunk-1 of chunk c; va holds batch 0 on entry.  The next
+        // batch's loads are issued before the current batch's additions.
+        const float* p = slot_ptr(c);
+        for (int i = 0; i < kBatchesPerChunk - 2; i += 2) {
 #pragma unroll
-                for (int q = 0; q < 16; ++q) sum = sum + v[q];
-            }
-            for (; r < cnt; ++r) sum = sum + b[r * kIcpVals + lane];
+            for (int q = 0; q < kBatch; ++q) vb[q] = p[((i + 1) * kBatch + q) * kIcpVals];
+#pragma unroll
+            for (int q = 0; q < kBatch; ++q) sum = sum + va[q];
+#pragma unroll
+            for (int q = 0; q < kBatch; ++q) va[q] = p[((i + 2) * kBatch + q) * kIcpVals];
+#pragma unroll
+            for (int q = 0; q < kBatch; ++q) sum = sum + vb[q];
         }
+#pragma unroll
+        for (int q = 0; q < kBatch; ++q) vb[q] = p[((kBatchesPerChunk - 1) * kBatch + q) * kIcpVals];
+#pragma unroll
+        for (int q = 0; q < kBatch; ++q) sum = sum + va[q];
+        // open the next full chunk before the last batch's additions
+        if (c + 1 < full) {
+            ok = bar_wait(&bars[(c + 1) % kBuffers], ((c + 1) / kBuffers) & 1);
+            const float* pn = slot_ptr(c + 1);
+#pragma unroll
+            for (int q = 0; q < kBatch; ++q) va[q] = ok ? pn[q * kIcpVals] : 0.f;
+        }
+#pragma unroll
+        for (int q = 0; q < kBatch; ++q) sum = sum + vb[q];
+        // every group of chunk c is added: its slot goes back to the copy engine
         __syncwarp();
-        if (lane == 0 && c + 2 < nchunks) {
-            // the warp's reads of this buffer precede the async-proxy write that refills it
+        if (lane == 0 && c + kBuffers < nchunks) {
+            // the warp's reads of this slot precede the async-proxy write that refills it
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            bulk_load(buf + (c & 1) * kChunkGroups * kIcpVals, partials + (size_t)(c + 2) * kChunkGroups * kIcpVals,
-                      chunk_bytes(c + 2), &bars[c & 1]);
+            bulk_load(buf + (c % kBuffers) * kChunkGroups * kIcpVals,
+                      partials + (size_t)(c + kBuffers) * kChunkGroups * kIcpVals, chunk_bytes(c + kBuffers),
+                      &bars[c % kBuffers]);
+        }
+    }
+    if (ok && full < nchunks) {
+        // the last, partial chunk, in batches without prefetch
+        if (full > 0) ok = bar_wait(&bars[full % kBuffers], (full / kBuffers) & 1);
+        if (ok) {
+            const float* p = slot_ptr(full);
+            const int cnt = ngroups - full * kChunkGroups;
+            int r = 0;
+            for (; r + kBatch <= cnt; r += kBatch) {
+#pragma unroll
+                for (int q = 0; q < kBatch; ++q) va[q] = p[(r + q) * kIcpVals];
+#pragma unroll
+                for (int q = 0; q < kBatch; ++q) sum = sum + va[q];
+            }
+            for (; r < cnt; ++r) sum = sum + p[r * kIcpVals];
         }
     }
     if (!ok) {
@@ -544,7 +611,7 @@ __global__ void __launch_bounds__(32, 1) icp_solve_kernel(const float* __restric
         // wait, and leave the pose as it is
         if (lane == 0) {
             st->error = 1;
-            for (int k = 0; k < 2; ++k) bar_wait(&bars[k], 0);
+            for (int k = 0; k < kBuffers; ++k) bar_wait(&bars[k], 0);
         }
         return;
     }
@@ -554,10 +621,15 @@ __global__ void __launch_bounds__(32, 1) icp_solve_kernel(const float* __restric
         if (lane < kIcpVals) sums_out[lane] = red[lane];
         return;
     }
-    finish_iteration_warp(st, prm, red);
+    if (lane < 16) {
+        sT0[lane] = t0;
+        sTp[lane] = tp;
+    }
+    __syncwarp();
+    finish_iteration_warp(st, prm, red, sT0, sTp, it);
 }
 
-size_t solve_smem_bytes(int /*ngroups*/) { return (size_t)2 * kChunkBytes; }
+size_t solve_smem_bytes(int /*ngroups*/) { return (size_t)kBuffers * kChunkBytes; }
 
 // the reduce-and-solve warp needs more than the default 48 KB of dynamic shared memory
 void ensure_solve_smem(int ngroups)
@@ -613,9 +685,10 @@ void launch_icp_iteration(const float4* vmap, const float4* nmap, const float4* 
     if (!prm.precise && prm.reference_order) {
         const int ng = icp_groups(cam.H, cam.W);
         ensure_solve_smem(ng);
-        icp_group_kernel<0><<<exact_blocks(cam.H, cam.W), kExactWarps * 32, 0, s>>>(
-            vmap, nmap, pv, pn, cam, prm, state_F(st), state_T(st), partials, list, ng, nullptr);
-        icp_solve_kernel<0><<<1, 32, solve_smem_bytes(ng), s>>>(partials, ng, st, prm, nullptr);
+        launch_pdl(icp_group_kernel<0>, dim3(exact_blocks(cam.H, cam.W)), dim3(kExactWarps * 32), 0, s, vmap, nmap, pv,
+                   pn, cam, prm, state_F(st), state_T(st), partials, list, ng, (int32_t*)nullptr);
+        launch_pdl(icp_solve_kernel<0>, dim3(1), dim3(32), solve_smem_bytes(ng), s, (const float*)partials, ng, st,
+                   prm, (float*)nullptr);
     } else if (prm.precise)
         icp_kernel<true, 0><<<blocks, kIcpBlock, 0, s>>>(vmap, nmap, pv, pn, cam, prm, st, state_F(st),
                                                          state_T(st), partials, nullptr, nullptr);
@@ -632,9 +705,10 @@ void launch_icp_associate(const float4* vmap, const float4* nmap, const float4* 
     if (!prm.precise && prm.reference_order) {
         const int ng = icp_groups(cam.H, cam.W);
         ensure_solve_smem(ng);
-        icp_group_kernel<1><<<exact_blocks(cam.H, cam.W), kExactWarps * 32, 0, s>>>(vmap, nmap, pv, pn, cam, prm, F,
-                                                                                    T, partials, list, ng, pair);
-        icp_solve_kernel<1><<<1, 32, solve_smem_bytes(ng), s>>>(partials, ng, st, prm, sums_out);
+        launch_pdl(icp_group_kernel<1>, dim3(exact_blocks(cam.H, cam.W)), dim3(kExactWarps * 32), 0, s, vmap, nmap, pv,
+                   pn, cam, prm, F, T, partials, list, ng, pair);
+        launch_pdl(icp_solve_kernel<1>, dim3(1), dim3(32), solve_smem_bytes(ng), s, (const float*)partials, ng, st,
+                   prm, sums_out);
     } else if (prm.precise)
         icp_kernel<true, 1><<<blocks, kIcpBlock, 0, s>>>(vmap, nmap, pv, pn, cam, prm, st, F, T, partials, sums_out,
                                                          pair);

@@ -51,14 +51,20 @@ void launch_integrate_f32(float* tsdf, float* weight, const float2* tab, const S
 void launch_integrate_f16(__half2* vol, const float2* tab, const State* st, const Grid& g, const Camera& cam,
                           long long skip_from, bool first, cudaStream_t s);
 
-// Amanatides-Woo ray cast (voxel_traversal.cu:75-424); hit may be nullptr
+// Amanatides-Woo ray cast (voxel_traversal.cu:75-424); hit may be nullptr; tile_counter
+// points to two device unsigneds, zero before the first launch, with which the persistent
+// kernel hands out ray tiles (the kernel leaves them at zero again)
 void launch_raycast_f32(const float* tsdf, const float* depth, float4* pv, float4* pn, int32_t* hit,
-                        const Camera& cam, const Grid& g, const State* st, cudaStream_t s);
+                        const Camera& cam, const Grid& g, const State* st, unsigned* tile_counter, cudaStream_t s);
 void launch_raycast_f16(const __half2* vol, const float* depth, float4* pv, float4* pn, int32_t* hit,
-                        const Camera& cam, const Grid& g, const State* st, cudaStream_t s);
+                        const Camera& cam, const Grid& g, const State* st, unsigned* tile_counter, cudaStream_t s);
+// once per device, outside any stream capture: sizes the persistent ray-cast grid
+int raycast_blocks();
 
 // st->c_flip from the device's own double acos (single thread, once per handle)
 void launch_calibrate(State* st, cudaStream_t s);
+// identity pose, zeroed ICP bookkeeping and error flag (c_flip kept)
+void launch_state_reset(State* st, cudaStream_t s);
 
 // volume layout conversions between the device x-fastest order and the reference's
 // z-fastest order

@@ -178,4 +178,39 @@ KF_HD void increment(const float* x, float* inc)
     inc[12] = 0.0f; inc[13] = 0.0f; inc[14] = 0.0f; inc[15] = 1.0f;
 }
 
+#if defined(__CUDACC__)
+// (float)(1. / sqrt(s)) for a double s -- the Cholesky pivot of hal::Cholesky32f --
+// bit for bit, mostly without the FP64 square root and division (about 900 dependent
+// cycles on a GPU with reduced FP64 throughput).  Ziv's strategy: an approximation
+// with a proven error bound decides the float rounding unless it lies too close to a
+// rounding boundary; only then is the exact FP64 expression evaluated.
+//   y0 = rsqrtf((float)s)                      relative error <= 2^-24 + 2 ulp < 2^-21
+//   e  = 1 - s*y0*y0   (y0*y0 exact in double; the product rounds by <= 2^-53; the
+//                       subtraction is exact by Sterbenz since s*y0*y0 is near 1)
+//   1/sqrt(s) = y0 (1 - e)^(-1/2) = y0 (1 + e/2 + 3e^2/8 + ...)
+//   c  = y0 * (e/2) in float; y0 + c approximates 1/sqrt(s) within 2^-42 relative
+//   (truncation 3e^2/8 < 2^-43, roundings of e and c < 2^-45 each).
+// f = fl(y0 + c) and err = (y0 + c) - f exactly (Fast2Sum, |y0| > |c|).  The FP64
+// expression is within 2^-52 of 1/sqrt(s), so when err keeps a margin of 2^-36 |f|
+// from the half-gap to f's neighbour on its side, both round to f.
+__device__ __forceinline__ float rsqrt_pivot(double s)
+{
+    if (s >= 1e-30 && s <= 1e30) {
+        const float y0 = rsqrtf((float)s);
+        const double y2 = (double)y0 * (double)y0;
+        const double e = 1.0 - s * y2;
+        if (fabs(e) < 0x1p-18) {
+            const float c = y0 * (0.5f * (float)e);
+            const float f = y0 + c;
+            const float err = c - (f - y0);
+            const int bits = __float_as_int(f);
+            const float half_gap = err >= 0.f ? 0.5f * (__int_as_float(bits + 1) - f)
+                                              : 0.5f * (f - __int_as_float(bits - 1));
+            if (fabsf(err) + f * 0x1p-36f < half_gap) return f;
+        }
+    }
+    return (float)(1. / sqrt(s));
+}
+#endif
+
 }  // namespace kf

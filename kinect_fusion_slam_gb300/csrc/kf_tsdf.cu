@@ -10,6 +10,7 @@
 // walked one thread per (x, y) column segment with x fastest, so a warp's updates are
 // 32 consecutive voxels.
 #include "kf_kernels.h"
+#include "kf_launch.cuh"
 
 namespace kf {
 
@@ -58,6 +59,7 @@ struct ViewF16 {
 __global__ void __launch_bounds__(256) integrate_prep_kernel(const float* __restrict__ depth, float2* __restrict__ tab,
                                                              Camera cam, State* st)
 {
+    wait_for_producer();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const float* K = cam.K;
     const float* Ki = cam.Ki;
@@ -102,6 +104,7 @@ __global__ void __launch_bounds__(kIntTx* kIntTy) integrate_kernel(Vol vol, cons
                                                                    float fy, float cx, float cy, int H, int W,
                                                                    int zchunk, long long skip_from)
 {
+    wait_for_producer();
     const int x = blockIdx.x * kIntTx + threadIdx.x;
     const int y = blockIdx.y * kIntTy + threadIdx.y;
     if (x >= g.dx || y >= g.dy) return;
@@ -320,6 +323,14 @@ __device__ __forceinline__ void trace(const View& vol, float X, float Y, float D
         return (unsigned)(a - 1) < (unsigned)(L - 2) && (unsigned)(b - 1) < (unsigned)(Wd - 2) &&
                (unsigned)(c - 1) < (unsigned)(Hz - 2);
     };
+    // The Amanatides-Woo step (:384-417) without branches: the same three comparisons
+    // pick the axis; selects apply the step.
+    auto pick = [](float3 t, bool& bx, bool& by, bool& bz) {
+        const bool xy = t.x < t.y, xz = t.x < t.z, yz = t.y < t.z;
+        bx = xy && xz;
+        by = !xy && yz;
+        bz = !(bx || by);
+    };
     // The stepping never depends on the loaded values, only the termination does, so a
     // lead walker with the same arithmetic runs kAhead steps in front and issues the
     // loads early into a register ring; the trailing walk consumes them in order.  The
@@ -328,27 +339,16 @@ __device__ __forceinline__ void trace(const View& vol, float X, float Y, float D
     int ax = ix, ay = iy, az = iz, ali = li;
     float3 atm = tm;
     auto lead_step = [&]() {
-        if (atm.x < atm.y) {
-            if (atm.x < atm.z) {
-                ax += sx;
-                ali += dlx;
-                atm.x = atm.x + td.x;
-            } else {
-                az += sz;
-                ali += dlz;
-                atm.z = atm.z + td.z;
-            }
-        } else {
-            if (atm.y < atm.z) {
-                ay += sy;
-                ali += dly;
-                atm.y = atm.y + td.y;
-            } else {
-                az += sz;
-                ali += dlz;
-                atm.z = atm.z + td.z;
-            }
-        }
+        bool bx, by, bz;
+        pick(atm, bx, by, bz);
+        ax += bx ? sx : 0;
+        ay += by ? sy : 0;
+        az += bz ? sz : 0;
+        ali += bx ? dlx : (by ? dly : dlz);
+        const float nx = atm.x + td.x, ny = atm.y + td.y, nz = atm.z + td.z;
+        atm.x = bx ? nx : atm.x;
+        atm.y = by ? ny : atm.y;
+        atm.z = bz ? nz : atm.z;
     };
     float ring[kAhead];
 #pragma unroll
@@ -356,12 +356,11 @@ __device__ __forceinline__ void trace(const View& vol, float X, float Y, float D
         ring[k] = inside_grid(ax, ay, az) ? vol.value(ali) : 0.f;
         lead_step();
     }
-
     float prev = 0.0f;
     float crossing = 0.f;  // the negative value met right after a positive one, or 0
     bool done = false;
-    // every iteration moves one index one step in a fixed direction, so the walk ends
-    // within L + Wd + Hz steps; the bound only makes that explicit
+    // every step moves one index one step in a fixed direction, so the walk ends within
+    // L + Wd + Hz steps; the bound only makes that explicit
     for (int guard = 0; !done && guard < L + Wd + Hz + 4; guard += kAhead) {
 #pragma unroll
         for (int k = 0; k < kAhead; ++k) {
@@ -373,17 +372,12 @@ __device__ __forceinline__ void trace(const View& vol, float X, float Y, float D
             ring[k] = inside_grid(ax, ay, az) ? vol.value(ali) : 0.f;
             lead_step();
             // the reference's four tests (:207-222) are mutually exclusive in prev
-            if (prev < 0.f) {
-                if (!(cur <= 0.f)) {  // NaN or back face
-                    done = true;
-                    break;
-                }
-            } else if (isnan(prev)) {
-                if (cur < 0.f) {
-                    done = true;
-                    break;
-                }
-            } else if (prev > 0.f && cur < 0.f) {
+            const bool stop = prev < 0.f ? !(cur <= 0.f) : (isnan(prev) && cur < 0.f);
+            if (stop) {
+                done = true;
+                break;
+            }
+            if (prev > 0.f && cur < 0.f) {
                 // zero crossing: leave the walk with the state as it is and resolve it
                 // below, where the warp's lanes have reconverged
                 crossing = cur;
@@ -391,36 +385,23 @@ __device__ __forceinline__ void trace(const View& vol, float X, float Y, float D
                 break;
             }
             prev = cur;
-            // Amanatides-Woo step (:384-417)
-            if (tm.x < tm.y) {
-                if (tm.x < tm.z) {
-                    ix += sx;
-                    li += dlx;
-                    XY = iy;
-                    XZ = iz;
-                    tm.x = tm.x + td.x;
-                } else {
-                    iz += sz;
-                    li += dlz;
-                    ZX = ix;
-                    ZY = iy;
-                    tm.z = tm.z + td.z;
-                }
-            } else {
-                if (tm.y < tm.z) {
-                    iy += sy;
-                    li += dly;
-                    YX = ix;
-                    YZ = iz;
-                    tm.y = tm.y + td.y;
-                } else {
-                    iz += sz;
-                    li += dlz;
-                    ZX = ix;
-                    ZY = iy;
-                    tm.z = tm.z + td.z;
-                }
-            }
+            bool bx, by, bz;
+            pick(tm, bx, by, bz);
+            const int ox = ix, oy = iy, oz = iz;
+            XY = bx ? oy : XY;
+            XZ = bx ? oz : XZ;
+            YX = by ? ox : YX;
+            YZ = by ? oz : YZ;
+            ZX = bz ? ox : ZX;
+            ZY = bz ? oy : ZY;
+            ix += bx ? sx : 0;
+            iy += by ? sy : 0;
+            iz += bz ? sz : 0;
+            li += bx ? dlx : (by ? dly : dlz);
+            const float nx = tm.x + td.x, ny = tm.y + td.y, nz = tm.z + td.z;
+            tm.x = bx ? nx : tm.x;
+            tm.y = by ? ny : tm.y;
+            tm.z = bz ? nz : tm.z;
         }
     }
     if (!(crossing < 0.f)) return;
@@ -475,41 +456,74 @@ __device__ __forceinline__ void trace(const View& vol, float X, float Y, float D
     oh = ((ix - 1) * Wd + (iy - 1)) * Hz + (iz - 1);
 }
 
-constexpr int kRayTile = 16;
+// Persistent: each warp takes 8x4-pixel tiles (one ray per lane) from a counter until
+// none are left, so the spatially clustered long walks do not leave a tail of idle SMs.
+// Tiles are numbered row-major, so consecutive tiles are neighbours in the image.
+constexpr int kRayBlock = 256;
 
-// 256 threads per 16x16 pixel tile; each warp covers an 8x4 sub-tile so that its rays
-// walk neighbouring voxels.
 template <class View>
-__global__ void __launch_bounds__(256) raycast_kernel(View vol, const float* __restrict__ depth,
-                                                      float4* __restrict__ pv, float4* __restrict__ pn,
-                                                      int32_t* __restrict__ hit, Camera cam, Grid g,
-                                                      const State* __restrict__ st)
+__global__ void __launch_bounds__(kRayBlock, 4) raycast_kernel(View vol, const float* __restrict__ depth,
+                                                            float4* __restrict__ pv, float4* __restrict__ pn,
+                                                            int32_t* __restrict__ hit, Camera cam, Grid g,
+                                                            const State* __restrict__ st, unsigned* tile_counter)
 {
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int px = blockIdx.x * kRayTile + (w & 1) * 8 + (lane & 7);
-    const int py = blockIdx.y * kRayTile + (w >> 1) * 4 + (lane >> 3);
-    if (px >= cam.W || py >= cam.H) return;
-    const int i = py * cam.W + px;
-    float4 op = make_float4(0.f, 0.f, 0.f, 0.f), on = op;
-    int oh = -1;
-    const float D = depth[i];
-    if (D != 0) {
-        float T[12];
+    wait_for_producer();
+    const int lane = threadIdx.x & 31;
+    const int tiles_x = (cam.W + 7) / 8, ntiles = tiles_x * ((cam.H + 3) / 4);
+    float T[12];
 #pragma unroll
-        for (int k = 0; k < 12; ++k) T[k] = st->T[k];
-        trace(vol, (float)px + 1.0f, (float)py + 1.0f, D, cam.Ki, T, g, st->c_flip, op, on, oh);
+    for (int k = 0; k < 12; ++k) T[k] = st->T[k];
+    const float c_flip = st->c_flip;
+    for (;;) {
+        unsigned tile = 0;
+        if (lane == 0) tile = atomicAdd(tile_counter, 1u);
+        tile = __shfl_sync(0xffffffffu, tile, 0);
+        if (tile >= (unsigned)ntiles) {
+            // the last warp out resets both counters for the next launch
+            if (lane == 0) {
+                const unsigned warps = gridDim.x * (blockDim.x / 32);
+                if (atomicAdd(tile_counter + 1, 1u) == warps - 1) {
+                    tile_counter[0] = 0u;
+                    tile_counter[1] = 0u;
+                }
+            }
+            return;
+        }
+        const int px = (int)(tile % tiles_x) * 8 + (lane & 7);
+        const int py = (int)(tile / tiles_x) * 4 + (lane >> 3);
+        if (px >= cam.W || py >= cam.H) continue;
+        const int i = py * cam.W + px;
+        float4 op = make_float4(0.f, 0.f, 0.f, 0.f), on = op;
+        int oh = -1;
+        const float D = depth[i];
+        if (D != 0) trace(vol, (float)px + 1.0f, (float)py + 1.0f, D, cam.Ki, T, g, c_flip, op, on, oh);
+        pv[i] = op;
+        pn[i] = on;
+        if (hit) hit[i] = oh;
     }
-    pv[i] = op;
-    pn[i] = on;
-    if (hit) hit[i] = oh;
 }
 
 }  // namespace
 
+int raycast_blocks()
+{
+    static int blocks[64] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64) return 152 * 4;
+    if (!blocks[dev]) {
+        int sms = 0, per_sm = 0;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, raycast_kernel<ViewF32>, kRayBlock, 0);
+        blocks[dev] = (sms > 0 ? sms : 152) * (per_sm > 0 ? per_sm : 4);
+    }
+    return blocks[dev];
+}
+
 void launch_integrate_prep(const float* depth, float2* tab, const Camera& cam, State* st, cudaStream_t s)
 {
     const int n = cam.H * cam.W;
-    integrate_prep_kernel<<<(n + 255) / 256, 256, 0, s>>>(depth, tab, cam, st);
+    launch_pdl(integrate_prep_kernel, dim3((n + 255) / 256), dim3(256), 0, s, depth, tab, cam, st);
 }
 
 namespace {
@@ -523,11 +537,11 @@ void integrate_launch(Vol vol, const float2* tab, const State* st, const Grid& g
     dim3 grid((g.dx + kIntTx - 1) / kIntTx, (g.dy + kIntTy - 1) / kIntTy, (g.dz + kZChunk - 1) / kZChunk);
     const float fx = cam.K[0], fy = cam.K[4], cx = cam.K[2], cy = cam.K[5];
     if (first)
-        integrate_kernel<Vol, true><<<grid, block, 0, s>>>(vol, tab, st, g, fx, fy, cx, cy, cam.H, cam.W, kZChunk,
-                                                           skip_from);
+        launch_pdl(integrate_kernel<Vol, true>, grid, block, 0, s, vol, tab, st, g, fx, fy, cx, cy, cam.H, cam.W,
+                   kZChunk, skip_from);
     else
-        integrate_kernel<Vol, false><<<grid, block, 0, s>>>(vol, tab, st, g, fx, fy, cx, cy, cam.H, cam.W, kZChunk,
-                                                            skip_from);
+        launch_pdl(integrate_kernel<Vol, false>, grid, block, 0, s, vol, tab, st, g, fx, fy, cx, cy, cam.H, cam.W,
+                   kZChunk, skip_from);
 }
 }  // namespace
 
@@ -544,17 +558,17 @@ void launch_integrate_f16(__half2* vol, const float2* tab, const State* st, cons
 }
 
 void launch_raycast_f32(const float* tsdf, const float* depth, float4* pv, float4* pn, int32_t* hit,
-                        const Camera& cam, const Grid& g, const State* st, cudaStream_t s)
+                        const Camera& cam, const Grid& g, const State* st, unsigned* tile_counter, cudaStream_t s)
 {
-    dim3 grid((cam.W + kRayTile - 1) / kRayTile, (cam.H + kRayTile - 1) / kRayTile);
-    raycast_kernel<<<grid, 256, 0, s>>>(ViewF32{tsdf}, depth, pv, pn, hit, cam, g, st);
+    launch_pdl(raycast_kernel<ViewF32>, dim3(raycast_blocks()), dim3(kRayBlock), 0, s, ViewF32{tsdf}, depth, pv, pn,
+               hit, cam, g, st, tile_counter);
 }
 
 void launch_raycast_f16(const __half2* vol, const float* depth, float4* pv, float4* pn, int32_t* hit,
-                        const Camera& cam, const Grid& g, const State* st, cudaStream_t s)
+                        const Camera& cam, const Grid& g, const State* st, unsigned* tile_counter, cudaStream_t s)
 {
-    dim3 grid((cam.W + kRayTile - 1) / kRayTile, (cam.H + kRayTile - 1) / kRayTile);
-    raycast_kernel<<<grid, 256, 0, s>>>(ViewF16{vol}, depth, pv, pn, hit, cam, g, st);
+    launch_pdl(raycast_kernel<ViewF16>, dim3(raycast_blocks()), dim3(kRayBlock), 0, s, ViewF16{vol}, depth, pv, pn,
+               hit, cam, g, st, tile_counter);
 }
 
 }  // namespace kf
