@@ -14,6 +14,7 @@
 
 #include "kf_kernels.h"
 #include "kf_launch.cuh"
+#include "kf_solve.cuh"
 
 namespace kf {
 
@@ -231,71 +232,20 @@ __device__ void finish_iteration_warp(State* st, const IcpParams& prm, const flo
         xb[lane] = sums[lane];
         for (int c = 0; c <= lane; ++c) L[lane * 6 + c] = sums[tri(c, lane)];  // lower triangle of A
     }
-    if (lane == 0) fail = 0;
     __syncwarp();
-    for (int j = 0; j < 6; ++j) {
-        // lanes j..5 accumulate row lane's entry of column j in one instruction stream:
-        // the diagonal subtracts the double square of each float, the off-diagonal the
-        // float product (cv::Cholesky's two inner loops), selected per lane
-        double sd = 0.0;
-        const int row = lane < 6 ? lane : 5;
-        if (lane >= j && lane < 6) {
-            sd = L[row * 6 + j];
-            for (int k = 0; k < j; ++k) {
-                const double t = L[row * 6 + k];
-                const double d_diag = t * t;
-                const double d_off = (double)(L[row * 6 + k] * L[j * 6 + k]);
-                sd -= lane == j ? d_diag : d_off;
-            }
-        }
-        if (lane == j) {
-            if (sd < FLT_EPSILON)
-                fail = 1;
-            else
-                L[j * 6 + j] = rsqrt_pivot(sd);
-        }
-        __syncwarp();
-        if (fail) break;
-        if (lane > j && lane < 6) L[lane * 6 + j] = (float)(sd * L[j * 6 + j]);
-        __syncwarp();
-    }
-    const bool ok = !fail;
+    const bool ok = warp_chol6(L, xb, &fail);
     if (lane == 0) {
-        if (ok) {
-            for (int i = 0; i < 6; ++i) {
-                double sd = xb[i];
-                for (int k = 0; k < i; ++k) sd -= L[i * 6 + k] * xb[k];
-                xb[i] = (float)(sd * L[i * 6 + i]);
-            }
-            for (int i = 5; i >= 0; --i) {
-                double sd = xb[i];
-                for (int k = 5; k > i; --k) sd -= L[k * 6 + i] * xb[k];
-                xb[i] = (float)(sd * L[i * 6 + i]);
-            }
-        } else if (prm.fail_mode == 1) {
+        if (!ok && prm.fail_mode == 1)
             for (int i = 0; i < 6; ++i) xb[i] = 0.f;
-        }
         increment(xb, inc);
     }
     __syncwarp();
-    // T <- Inc * T and F <- T_prev^-1 * T, one output entry per lane (kf::mat4's order)
-    if (lane < 16) {
-        const int r = lane >> 2, c = lane & 3;
-        double a = (double)inc[r * 4 + 0] * T0[c];
-        a += (double)inc[r * 4 + 1] * T0[4 + c];
-        a += (double)inc[r * 4 + 2] * T0[8 + c];
-        a += (double)inc[r * 4 + 3] * T0[12 + c];
-        Tn[lane] = (float)a;
-    }
+    // T <- Inc * T and F <- T_prev^-1 * T, one output entry per lane
+    if (lane < 16) Tn[lane] = mat4_entry(inc, T0, lane);
     __syncwarp();
     if (lane < 16) {
         st->T[lane] = Tn[lane];
-        const int r = lane >> 2, c = lane & 3;
-        double a = (double)Tprev_inv[r * 4 + 0] * Tn[c];
-        a += (double)Tprev_inv[r * 4 + 1] * Tn[4 + c];
-        a += (double)Tprev_inv[r * 4 + 2] * Tn[8 + c];
-        a += (double)Tprev_inv[r * 4 + 3] * Tn[12 + c];
-        st->F[lane] = (float)a;
+        st->F[lane] = mat4_entry(Tprev_inv, Tn, lane);
     }
     if (it < kMaxIcpIters && lane < 16) st->Tlog[it][lane] = Tn[lane];
     if (lane < kIcpVals) st->sums[lane] = sums[lane];
@@ -557,20 +507,25 @@ __global__ void __launch_bounds__(32, 1) icp_solve_kernel(const float* __restric
         // batches 0..kBatchesPerChunk-1 of chunk c; va holds batch 0 on entry.  The next
         // batch's loads are issued before the current batch's additions.
         const float* p = slot_ptr(c);
+        // each load is issued between two dependent additions, in the issue slots the
+        // FADD latency leaves free
         for (int i = 0; i < kBatchesPerChunk - 2; i += 2) {
 #pragma unroll
-            for (int q = 0; q < kBatch; ++q) vb[q] = p[((i + 1) * kBatch + q) * kIcpVals];
+            for (int q = 0; q < kBatch; ++q) {
+                vb[q] = p[((i + 1) * kBatch + q) * kIcpVals];
+                sum = sum + va[q];
+            }
 #pragma unroll
-            for (int q = 0; q < kBatch; ++q) sum = sum + va[q];
-#pragma unroll
-            for (int q = 0; q < kBatch; ++q) va[q] = p[((i + 2) * kBatch + q) * kIcpVals];
-#pragma unroll
-            for (int q = 0; q < kBatch; ++q) sum = sum + vb[q];
+            for (int q = 0; q < kBatch; ++q) {
+                va[q] = p[((i + 2) * kBatch + q) * kIcpVals];
+                sum = sum + vb[q];
+            }
         }
 #pragma unroll
-        for (int q = 0; q < kBatch; ++q) vb[q] = p[((kBatchesPerChunk - 1) * kBatch + q) * kIcpVals];
-#pragma unroll
-        for (int q = 0; q < kBatch; ++q) sum = sum + va[q];
+        for (int q = 0; q < kBatch; ++q) {
+            vb[q] = p[((kBatchesPerChunk - 1) * kBatch + q) * kIcpVals];
+            sum = sum + va[q];
+        }
         // open the next full chunk before the last batch's additions
         if (c + 1 < full) {
             ok = bar_wait(&bars[(c + 1) % kBuffers], ((c + 1) / kBuffers) & 1);
