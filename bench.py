@@ -49,11 +49,13 @@ def parse_args(argv=None):
     p.add_argument("--warmup", type=int, default=10)
     p.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     p.add_argument("--config", default="c1")
-    p.add_argument("--tsdf", choices=["f32", "f16"], default="f32")
+    p.add_argument("--form", choices=["both", "precision", "plain"], default="both",
+                   help="precision: FP16 TSDF, compensated one-pass sums, FP64 solve; plain: the bit-exact FP32 form")
     p.add_argument("--profile-frames", type=int, default=30, help="frames with per-stage CUDA events")
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample budget")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-ate", action="store_true", help="skip the trajectory comparison with the FP64 oracle")
     return p.parse_args(argv)
 
 
@@ -177,10 +179,10 @@ def config_desc(cfg, args) -> dict:
         "workload": (f"{cfg.name}: {cfg.camera.width}x{cfg.camera.height} uint16 depth, "
                      f"{g.dims[0]}x{g.dims[1]}x{g.dims[2]} TSDF @ {g.voxel_size:g} mm, single-level ICP x10, "
                      "integration + ray cast per frame"),
-        "tsdf": args.tsdf,
         "frames_unique": UNIQUE_FRAMES,
-        "l2": f"TSDF {'pair' if args.tsdf == 'f32' else 'half2'} of {g.nvox * (8 if args.tsdf == 'f32' else 4) / 1e6:.0f} MB "
-              "> 129 MB L2 (inputs larger than L2, no flush)",
+        "restart_every": 2 * (UNIQUE_FRAMES - 1),
+        "l2": f"TSDF pair of {g.nvox * 8 / 1e6:.0f} MB (FP32) / {g.nvox * 4 / 1e6:.0f} MB (FP16) > 129 MB L2 "
+              "(inputs larger than L2, no flush)",
         "parallelism": f"replicas x{args.gpus}",
     }
 
@@ -257,33 +259,60 @@ def read_profile_traffic(kernel: str):
     return None
 
 
-def run_gb300(args, dist: Dist):
+FORMS = {
+    # bit-exact drop-in: FP32 TSDF, the reference's 64-wide + serial summation order and
+    # float Cholesky
+    "plain": {"tsdf": "f32", "reduction": "reference", "solve": "reference"},
+    # precision form: FP16 value + weight, compensated FP32 sums in one pass, FP64 solve
+    "precision": {"tsdf": "f16", "reduction": "tree", "solve": "precise"},
+}
+
+
+def form_config(kf, cfg, form: str):
+    g, cam = cfg.grid, cfg.camera
+    f = FORMS[form]
+    return kf.make_config(height=cam.height, width=cam.width, dims=g.dims, grid_start=g.start,
+                          voxel_size=g.voxel_size,
+                          tsdf_storage=kf.KF_TSDF_F16 if f["tsdf"] == "f16" else kf.KF_TSDF_F32,
+                          icp_reduction=kf.KF_REDUCE_TREE if f["reduction"] == "tree" else kf.KF_REDUCE_REFERENCE_ORDER,
+                          solve_mode=kf.KF_SOLVE_PRECISE if f["solve"] == "precise" else kf.KF_SOLVE_REFERENCE)
+
+
+def trajectory_error(h, dev, fbytes, n_frames: int):
+    """Absolute trajectory error (RMS and max translation difference, mm) of this handle's
+    pipeline over frames 0..n-1 against the FP64 oracle's trajectory stored in
+    tests/golden/fp64_c1_traj.npz; also the float oracle's (the reference's own
+    arithmetic) error against the same trajectory."""
+    p = ROOT / "tests" / "golden" / "fp64_c1_traj.npz"
+    if not p.exists():
+        return None
+    z = np.load(p)
+    n = min(n_frames, int(z["frames"]))
+    h.reset()
+    poses = np.zeros((n, 4, 4))
+    for k in range(n):
+        ptr = dev.data_ptr() + k * fbytes
+        (h.initial_processing_device if k == 0 else h.incoming_frame_device)(ptr)
+        poses[k] = h.pose()
+    e = np.linalg.norm(poses[:, :3, 3] - z["poses64"][:n, :3, 3], axis=1)
+    r = np.linalg.norm(z["poses32"][:n, :3, 3] - z["poses64"][:n, :3, 3], axis=1)
+    return {"frames": n, "ate_mm": float(np.sqrt(np.mean(e ** 2))), "max_mm": float(e.max()),
+            "reference_float_ate_mm": float(np.sqrt(np.mean(r ** 2)))}
+
+
+def run_form(args, dist, form, cfg, frames, order, fresh, stream):
     import torch
 
     import kinect_fusion_slam_gb300 as kf
-    from kinect_fusion_slam_gb300 import scene
 
-    torch.cuda.set_device(dist.local_rank)
-    cfg = workload(args)
-    g, cam = cfg.grid, cfg.camera
-    n_total = 1 + args.warmup + args.steps
-    seq = scene.sequence(cfg, frames=UNIQUE_FRAMES)
-    frames = seq.depths(UNIQUE_FRAMES)
-    n_all = n_total + args.profile_frames + (0 if args.no_e2e else args.steps)
-    order = pingpong(UNIQUE_FRAMES, n_all)
-    fresh = restarts(UNIQUE_FRAMES, n_all)
-    K = seq.K
-    storage = kf.KF_TSDF_F16 if args.tsdf == "f16" else kf.KF_TSDF_F32
-    conf = kf.make_config(height=cam.height, width=cam.width, dims=g.dims, grid_start=g.start,
-                          voxel_size=g.voxel_size, tsdf_storage=storage)
-    h = kf.Handle(conf)
+    cam = cfg.camera
+    h = kf.Handle(form_config(kf, cfg, form))
+    K = cfg.camera.K_reference()
     h.set_intrinsics(K[0, 0], K[1, 1], K[0, 2], K[1, 2])
-    # a dedicated stream: torch's default stream is the legacy NULL stream (handle 0)
-    stream = torch.cuda.Stream()
-    torch.cuda.set_stream(stream)
     h.set_stream(stream.cuda_stream)
     dev = torch.from_numpy(frames.view(np.int16)).cuda()
     fbytes = cam.height * cam.width * 2
+    n_total = 1 + args.warmup + args.steps
 
     def dptr(k):
         return dev.data_ptr() + order[k] * fbytes
@@ -311,14 +340,13 @@ def run_gb300(args, dist: Dist):
     torch.cuda.synchronize()
     clk = clocks.stop()
     dist.barrier()
-    ms = e0.elapsed_time(e1)
-    ms_max = dist.max(ms)
-    fps = args.steps * dist.world / (ms_max / 1000.0)
+    ms_max = dist.max(e0.elapsed_time(e1))
     kpf = h.kernels_per_frame()
     n_fresh = sum(fresh[1 + args.warmup:n_total])
-    # a restart: reset (two NaN fills for TSDF and weights, the state reset) and
+    # a restart: reset (two NaN fills or one for the FP16 pair, the state reset) and
     # InitialProcessing (vertex map, integration prep, integration, ray cast)
-    launches = kpf * (args.steps - n_fresh) + 7 * n_fresh
+    reset_kernels = 2 if FORMS[form]["tsdf"] == "f16" else 3
+    launches = kpf * (args.steps - n_fresh) + (4 + reset_kernels) * n_fresh
 
     # per-stage device time with CUDA events recorded inside each frame's graph
     # (incoming frames only: InitialProcessing has no ICP stage)
@@ -332,7 +360,6 @@ def run_gb300(args, dist: Dist):
     st = np.mean(np.array(stages), axis=0) if stages else np.zeros(5)
     stage_ms = {"vertex": float(st[0]), "icp": float(st[1]), "integration": float(st[2]), "raycast": float(st[3]),
                 "frame": float(st[4])}
-    nc, _ = h.icp_stats(10)
 
     # end to end through the C ABI with host buffers
     e2e = None
@@ -349,45 +376,88 @@ def run_gb300(args, dist: Dist):
             else:
                 h.incoming_frame_ptr(ptr)
             h.pose()
-        dt = time.perf_counter() - t0
-        dt = dist.max(dt)
+        dt = dist.max(time.perf_counter() - t0)
         e2e = {"value": args.steps * dist.world / dt, "unit": "frames/s", "h2d_bytes_per_step": fbytes,
                "d2h_bytes_per_step": 64}
 
-    # roofline of the dominant stage
-    nvox = g.nvox
-    bpv = 16 if args.tsdf == "f32" else 8
-    dominant = max(("integration", "icp", "raycast"), key=lambda s: stage_ms[s])
+    ate = trajectory_error(h, dev, fbytes, len(frames)) if not args.no_ate else None
+    h.close()
+    return {"value": args.steps * dist.world / (ms_max / 1000.0), "ms_per_step": ms_max / args.steps,
+            "e2e": e2e, "stages_ms": stage_ms, "gpu_launches": launches, "clocks": clk, "ate": ate,
+            "tsdf": FORMS[form]["tsdf"]}
+
+
+def roofline_of(cfg, r, tsdf: str):
+    """Roofline of the form's dominant stage from the live stage events; algorithmic
+    bytes per frame: integration 16 B/voxel (FP32 pair) or 8 B/voxel (FP16 pair) over
+    the whole grid; ray cast ~45 voxel reads per valid ray of 4 B (2 B FP16); ICP
+    49 B per pixel-iteration (10 iterations)."""
+    g, cam = cfg.grid, cfg.camera
+    st = r["stages_ms"]
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
     peak = float(peaks.get("hbm_gbs", 6800.0))
-    if dominant == "integration":
-        alg = bpv * nvox
-        kernel = "integrate_kernel"
-    elif dominant == "icp":
-        alg = 49 * cam.height * cam.width * 10
-        kernel = "icp_kernel"
-    else:
-        alg = 4 * 45 * int((frames[0] > 0).sum())
-        kernel = "raycast_kernel"
-    achieved = alg / (stage_ms[dominant] / 1000.0) / 1e9 if stage_ms[dominant] > 0 else 0.0
-    traffic = read_profile_traffic(kernel)
-    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": traffic, "kernel": kernel, "stage_ms": stage_ms[dominant],
-                "peak_source": "measured" if peaks else "fallback"}
+    alg = {
+        "integration": (16 if tsdf == "f32" else 8) * g.nvox,
+        "icp": 49 * cam.height * cam.width * 10,
+        "raycast": 45 * (4 if tsdf == "f32" else 2) * int(0.83 * cam.height * cam.width),
+    }
+    kernels = {"integration": "integrate_kernel", "icp": "icp_group_kernel" if tsdf == "f32" else "icp_kernel",
+               "raycast": "raycast_kernel"}
+    stages = {}
+    for s in ("integration", "icp", "raycast"):
+        ach = alg[s] / (st[s] / 1000.0) / 1e9 if st[s] > 0 else 0.0
+        stages[s] = {"achieved": ach, "frac": ach / peak, "ms": st[s], "alg_bytes": alg[s]}
+    dom = max(stages, key=lambda s: stages[s]["ms"])
+    return {"bound": "hbm", "achieved": stages[dom]["achieved"], "peak": peak, "unit": "GB/s",
+            "frac": stages[dom]["frac"], "traffic": read_profile_traffic(kernels[dom]), "kernel": kernels[dom],
+            "stage": dom, "peak_source": "measured" if peaks else "fallback",
+            "stages": {k: {kk: round(vv, 4) for kk, vv in v.items()} for k, v in stages.items()}}
+
+
+def run_gb300(args, dist: Dist):
+    import torch
+
+    from kinect_fusion_slam_gb300 import scene
+
+    torch.cuda.set_device(dist.local_rank)
+    cfg = workload(args)
+    n_total = 1 + args.warmup + args.steps
+    seq = scene.sequence(cfg, frames=UNIQUE_FRAMES)
+    frames = seq.depths(UNIQUE_FRAMES)
+    n_all = n_total + args.profile_frames + (0 if args.no_e2e else args.steps)
+    order = pingpong(UNIQUE_FRAMES, n_all)
+    fresh = restarts(UNIQUE_FRAMES, n_all)
+    # a dedicated stream: torch's default stream is the legacy NULL stream (handle 0)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    forms = ["precision", "plain"] if args.form == "both" else [args.form]
+    res = {f: run_form(args, dist, f, cfg, frames, order, fresh, stream) for f in forms}
+    head = res[forms[0]]
 
     cb = None
     if dist.rank == 0 and args.gpus == 1 and not args.no_cpu_baseline:
         cb = cpu_baseline(cfg, frames, order, args.cpu_seconds)
 
+    desc = config_desc(cfg, args)
+    desc["form"] = forms[0]
+    desc["tsdf"] = head["tsdf"]
     line = {
-        "metric": METRIC, "value": fps, "unit": "frames/s", "n_gpus": dist.world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": args.tsdf, "data": "synthetic: seeded analytic room, Kinect v1 noise",
-        "config": config_desc(cfg, args), "roofline": roofline, "cpu_baseline": cb, "e2e": e2e,
-        "gpu_launches": launches, "clocks": clk, "stages_ms": stage_ms,
-        "icp_correspondences_last_frame": [int(x) for x in nc],
+        "metric": METRIC, "value": head["value"], "unit": "frames/s", "n_gpus": dist.world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": head["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32 arithmetic, " + ("f16 TSDF value+weight" if head["tsdf"] == "f16" else "f32 TSDF"),
+        "data": "synthetic: seeded analytic room, Kinect v1 noise", "config": desc,
+        "roofline": roofline_of(cfg, head, head["tsdf"]), "cpu_baseline": cb, "e2e": head["e2e"],
+        "gpu_launches": head["gpu_launches"], "clocks": head["clocks"], "stages_ms": head["stages_ms"],
+        "ate": head["ate"],
     }
-    h.close()
+    if "plain" in res and forms[0] != "plain":
+        p = res["plain"]
+        line["fp32_form"] = {"value": p["value"], "ms_per_step": p["ms_per_step"], "e2e": p["e2e"],
+                             "stages_ms": p["stages_ms"], "ate": p["ate"], "gpu_launches": p["gpu_launches"],
+                             "roofline": roofline_of(cfg, p, "f32")}
+        line["speedup_vs_fp32_form"] = head["value"] / p["value"]
+        line["gpu_launches"] = head["gpu_launches"] + p["gpu_launches"]
     if dist.rank == 0:
         print(json.dumps(line), flush=True)
     dist.close()

@@ -160,66 +160,10 @@ __device__ __forceinline__ void block_reduce(Acc<PRECISE>& acc, float* sh_hi, fl
 __device__ __forceinline__ int tri(int r, int s) { return 6 + r * 6 - r * (r - 1) / 2 + (s - r); }
 
 // Solve the 6x6 system from the reduced sums, apply the small-angle increment to the
-// pose and prepare the next iteration (sensor_pose_estimation.cu:389-429).  One thread.
-template <bool PRECISE>
-__device__ void finish_iteration(State* st, const IcpParams& prm, const float* hi, const float* lo)
-{
-    const int it = st->iter;
-    for (int k = 0; k < kIcpVals; ++k) st->sums[k] = PRECISE ? hi[k] + lo[k] : hi[k];
-    bool ok;
-    if (!PRECISE) {
-        float A[36], x[6];
-        for (int r = 0; r < 6; ++r)
-            for (int s = r; s < 6; ++s) A[r * 6 + s] = A[s * 6 + r] = hi[tri(r, s)];
-        for (int r = 0; r < 6; ++r) x[r] = hi[r];
-        // cv::Cholesky; on failure the reference keeps b untouched and applies it
-        ok = chol6(A, x);
-        if (!ok && prm.fail_mode == 1)
-            for (int r = 0; r < 6; ++r) x[r] = 0.f;
-        float inc[16];
-        increment(x, inc);
-        mat4(inc, st->T, st->T);
-    } else {
-        double A[36], x[6];
-        for (int r = 0; r < 6; ++r)
-            for (int s = r; s < 6; ++s) A[r * 6 + s] = A[s * 6 + r] = (double)hi[tri(r, s)] + (double)lo[tri(r, s)];
-        for (int r = 0; r < 6; ++r) x[r] = (double)hi[r] + (double)lo[r];
-        ok = chol6_f64(A, x);
-        if (!ok) {
-            if (prm.fail_mode == 1)
-                for (int r = 0; r < 6; ++r) x[r] = 0.0;
-            else
-                for (int r = 0; r < 6; ++r) x[r] = (double)hi[r] + (double)lo[r];
-        }
-        // SE(3) composition in FP64: the same small-angle increment, applied to the FP64 pose
-        const double inc[16] = {1.0, x[2], -x[1], x[3], -x[2], 1.0, x[0], x[4],
-                                x[1], -x[0], 1.0, x[5], 0.0, 0.0, 0.0, 1.0};
-        double R[16];
-        for (int r = 0; r < 4; ++r)
-            for (int c = 0; c < 4; ++c) {
-                double acc = 0.0;
-                for (int k = 0; k < 4; ++k) acc += inc[r * 4 + k] * st->Td[k * 4 + c];
-                R[r * 4 + c] = acc;
-            }
-        for (int k = 0; k < 16; ++k) {
-            st->Td[k] = R[k];
-            st->T[k] = (float)R[k];
-        }
-    }
-    mat4(st->Tprev_inv, st->T, st->F);
-    if (it < kMaxIcpIters) {
-        st->ncorr[it] = (int32_t)(hi[kIcpVals - 1] + (PRECISE ? lo[kIcpVals - 1] : 0.f));
-        st->chol_ok[it] = ok ? 1 : 0;
-        for (int k = 0; k < 16; ++k) st->Tlog[it][k] = st->T[k];
-    }
-    st->iter = it + 1;
-}
-
-// The same solve and update as finish_iteration<false> with the work spread over the
-// 32 lanes of one warp (FP64 latency dominates this step on GB300): the Cholesky factor
-// is formed column by column -- each entry from the same operands in the same order as
-// cv::Cholesky's row-by-row loop, so every bit is the same -- and each entry of the two
-// 4x4 products is computed by its own lane.  All 32 lanes of the calling warp must call.
+// pose and prepare the next iteration (sensor_pose_estimation.cu:389-429), bit for bit
+// as cv::Cholesky and cv::Mat's product do it, by the 32 lanes of one warp (warp_chol6
+// and mat4_entry: FP64 latency dominates this step on GB300, so the double sums are
+// carried in float pairs).  All 32 lanes of the calling warp must call.
 // T0 and Tprev_inv: the state's T and Tprev_inv, already loaded by the caller (shared
 // memory), so their global-memory latency overlaps the reduction; it: the state's iter
 __device__ void finish_iteration_warp(State* st, const IcpParams& prm, const float* sums, const float* T0,
@@ -253,6 +197,64 @@ __device__ void finish_iteration_warp(State* st, const IcpParams& prm, const flo
     if (lane == 0) {
         if (it < kMaxIcpIters) {
             st->ncorr[it] = (int32_t)sums[kIcpVals - 1];
+            st->chol_ok[it] = ok ? 1 : 0;
+        }
+        st->iter = it + 1;
+    }
+}
+
+// The precision form's update by one warp: the compensated sums (hi + lo) as FP64, the
+// FP64 Cholesky solve, and the SE(3) composition Inc * T applied to the FP64 pose (the
+// only FP64 steps); the float pose and F follow from it.
+__device__ void finish_precise_warp(State* st, const IcpParams& prm, const float* hi, const float* lo)
+{
+    __shared__ double A[36], x[6], r[6], inc[16], Tn[16];
+    __shared__ float Tf[16], Tp[16];
+    __shared__ int fail;
+    const int lane = threadIdx.x & 31;
+    const int it = st->iter;
+    if (lane < 16) {
+        Tp[lane] = st->Tprev_inv[lane];
+        Tn[lane] = st->Td[lane];
+    }
+    if (lane < 6) {
+        x[lane] = (double)hi[lane] + (double)lo[lane];
+        for (int c = 0; c <= lane; ++c) A[lane * 6 + c] = (double)hi[tri(c, lane)] + (double)lo[tri(c, lane)];
+    }
+    if (lane < kIcpVals) st->sums[lane] = hi[lane] + lo[lane];
+    __syncwarp();
+    const bool ok = warp_chol6_f64(A, x, r, &fail);
+    if (lane == 0) {
+        if (!ok)  // the reference applies b as it stands, or the identity in that fail mode
+            for (int i = 0; i < 6; ++i) x[i] = prm.fail_mode == 1 ? 0.0 : (double)hi[i] + (double)lo[i];
+        const double e[16] = {1.0, x[2], -x[1], x[3], -x[2], 1.0, x[0], x[4],
+                              x[1], -x[0], 1.0, x[5], 0.0, 0.0, 0.0, 1.0};
+        for (int k = 0; k < 16; ++k) inc[k] = e[k];
+    }
+    __syncwarp();
+    double tn = 0.0;
+    if (lane < 16) {
+        const int rr = lane >> 2, c = lane & 3;
+        tn = inc[rr * 4] * Tn[c];
+        tn = fma(inc[rr * 4 + 1], Tn[4 + c], tn);
+        tn = fma(inc[rr * 4 + 2], Tn[8 + c], tn);
+        tn = fma(inc[rr * 4 + 3], Tn[12 + c], tn);
+    }
+    __syncwarp();
+    if (lane < 16) {
+        st->Td[lane] = tn;
+        Tf[lane] = (float)tn;
+        st->T[lane] = Tf[lane];
+    }
+    __syncwarp();
+    if (lane < 16) {
+        const float f = mat4_entry(Tp, Tf, lane);
+        st->F[lane] = f;
+        if (it < kMaxIcpIters) st->Tlog[it][lane] = Tf[lane];
+    }
+    if (lane == 0) {
+        if (it < kMaxIcpIters) {
+            st->ncorr[it] = (int32_t)(hi[kIcpVals - 1] + lo[kIcpVals - 1]);
             st->chol_ok[it] = ok ? 1 : 0;
         }
         st->iter = it + 1;
@@ -326,7 +328,7 @@ __global__ void __launch_bounds__(kIcpBlock) icp_kernel(const float4* __restrict
         return;
     }
     if (PRECISE) {
-        if (threadIdx.x == 0) finish_iteration<true>(st, prm, red_hi, red_lo);
+        finish_precise_warp(st, prm, red_hi, red_lo);
     } else {
         __shared__ float sT0[16], sTp[16];
         if (threadIdx.x < 16) {
@@ -584,6 +586,58 @@ __global__ void __launch_bounds__(32, 1) icp_solve_kernel(const float* __restric
     finish_iteration_warp(st, prm, red, sT0, sTp, it);
 }
 
+// The precision form's reduce-and-solve pass: one block of 32 warps.  The group sums
+// of the group pass are added with compensated (TwoSum) FP32 arithmetic -- warp w,
+// lane k accumulates term k over groups w, w + 32, ...; the 32 warp partials are then
+// combined the same way -- and warp 0 solves in FP64 (finish_precise_warp, MODE 0) or
+// writes hi + lo (MODE 1).  Summation order is free here: the precision form is held
+// to the FP64 oracle, not to the reference's bits.
+constexpr int kPreciseWarps = 32;
+
+template <int MODE>
+__global__ void __launch_bounds__(kPreciseWarps * 32, 1) icp_precise_reduce_kernel(
+    const float* __restrict__ partials, int ngroups, State* st, IcpParams prm, float* sums_out)
+{
+    wait_for_producer();
+    __shared__ float sh_hi[kPreciseWarps][kIcpVals], sh_lo[kPreciseWarps][kIcpVals];
+    __shared__ float red_hi[kIcpVals], red_lo[kIcpVals];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int term = lane < kIcpVals ? lane : kIcpVals - 1;
+    float h = 0.f, l = 0.f;
+#pragma unroll 8
+    for (int g = warp; g < ngroups; g += kPreciseWarps) {
+        const float v = __ldcg(partials + (size_t)g * kIcpVals + term);
+        float sum, e;
+        two_sum(h, v, sum, e);
+        h = sum;
+        l += e;
+    }
+    if (lane < kIcpVals) {
+        sh_hi[warp][lane] = h;
+        sh_lo[warp][lane] = l;
+    }
+    __syncthreads();
+    if (threadIdx.x < kIcpVals) {
+        const int k = threadIdx.x;
+        float H = sh_hi[0][k], L = sh_lo[0][k];
+        for (int w = 1; w < kPreciseWarps; ++w) {
+            float sum, e;
+            two_sum(H, sh_hi[w][k], sum, e);
+            H = sum;
+            L += e + sh_lo[w][k];
+        }
+        red_hi[k] = H;
+        red_lo[k] = L;
+    }
+    __syncthreads();
+    if (warp != 0) return;
+    if (MODE == 1) {
+        if (lane < kIcpVals) sums_out[lane] = red_hi[lane] + red_lo[lane];
+        return;
+    }
+    finish_precise_warp(st, prm, red_hi, red_lo);
+}
+
 size_t solve_smem_bytes(int /*ngroups*/) { return (size_t)kBuffers * kChunkBytes; }
 
 // the reduce-and-solve warp needs more than the default 48 KB of dynamic shared memory
@@ -644,10 +698,13 @@ void launch_icp_iteration(const float4* vmap, const float4* nmap, const float4* 
                    pn, cam, prm, state_F(st), state_T(st), partials, list, ng, (int32_t*)nullptr);
         launch_pdl(icp_solve_kernel<0>, dim3(1), dim3(32), solve_smem_bytes(ng), s, (const float*)partials, ng, st,
                    prm, (float*)nullptr);
-    } else if (prm.precise)
-        icp_kernel<true, 0><<<blocks, kIcpBlock, 0, s>>>(vmap, nmap, pv, pn, cam, prm, st, state_F(st),
-                                                         state_T(st), partials, nullptr, nullptr);
-    else
+    } else if (prm.precise) {
+        const int ng = icp_groups(cam.H, cam.W);
+        launch_pdl(icp_group_kernel<0>, dim3(exact_blocks(cam.H, cam.W)), dim3(kExactWarps * 32), 0, s, vmap, nmap, pv,
+                   pn, cam, prm, state_F(st), state_T(st), partials, list, ng, (int32_t*)nullptr);
+        launch_pdl(icp_precise_reduce_kernel<0>, dim3(1), dim3(kPreciseWarps * 32), 0, s, (const float*)partials, ng,
+                   st, prm, (float*)nullptr);
+    } else
         icp_kernel<false, 0><<<blocks, kIcpBlock, 0, s>>>(vmap, nmap, pv, pn, cam, prm, st, state_F(st),
                                                           state_T(st), partials, nullptr, nullptr);
 }
@@ -664,10 +721,13 @@ void launch_icp_associate(const float4* vmap, const float4* nmap, const float4* 
                    pn, cam, prm, F, T, partials, list, ng, pair);
         launch_pdl(icp_solve_kernel<1>, dim3(1), dim3(32), solve_smem_bytes(ng), s, (const float*)partials, ng, st,
                    prm, sums_out);
-    } else if (prm.precise)
-        icp_kernel<true, 1><<<blocks, kIcpBlock, 0, s>>>(vmap, nmap, pv, pn, cam, prm, st, F, T, partials, sums_out,
-                                                         pair);
-    else
+    } else if (prm.precise) {
+        const int ng = icp_groups(cam.H, cam.W);
+        launch_pdl(icp_group_kernel<1>, dim3(exact_blocks(cam.H, cam.W)), dim3(kExactWarps * 32), 0, s, vmap, nmap, pv,
+                   pn, cam, prm, F, T, partials, list, ng, pair);
+        launch_pdl(icp_precise_reduce_kernel<1>, dim3(1), dim3(kPreciseWarps * 32), 0, s, (const float*)partials, ng,
+                   st, prm, sums_out);
+    } else
         icp_kernel<false, 1><<<blocks, kIcpBlock, 0, s>>>(vmap, nmap, pv, pn, cam, prm, st, F, T, partials,
                                                           sums_out, pair);
 }

@@ -139,35 +139,6 @@ KF_HD bool chol6(float* A, float* b)
     return true;
 }
 
-// FP64 Cholesky solve of A x = b (precise solve mode); false when not positive definite
-KF_HD bool chol6_f64(double* A, double* b)
-{
-    const int m = 6;
-    for (int i = 0; i < m; ++i) {
-        for (int j = 0; j <= i; ++j) {
-            double s = A[i * m + j];
-            for (int k = 0; k < j; ++k) s -= A[i * m + k] * A[j * m + k];
-            if (i == j) {
-                if (!(s > 0.0)) return false;
-                A[i * m + i] = sqrt(s);
-            } else {
-                A[i * m + j] = s / A[j * m + j];
-            }
-        }
-    }
-    for (int i = 0; i < m; ++i) {
-        double s = b[i];
-        for (int k = 0; k < i; ++k) s -= A[i * m + k] * b[k];
-        b[i] = s / A[i * m + i];
-    }
-    for (int i = m - 1; i >= 0; --i) {
-        double s = b[i];
-        for (int k = i + 1; k < m; ++k) s -= A[k * m + i] * b[k];
-        b[i] = s / A[i * m + i];
-    }
-    return true;
-}
-
 // the small-angle increment of sensor_pose_estimation.cu:406-425,
 // x = (beta, gamma, alpha, tx, ty, tz)
 KF_HD void increment(const float* x, float* inc)

@@ -286,4 +286,61 @@ __device__ __forceinline__ float mat4_entry(const float* a, const float* b, int 
     return ff::mat4_entry_f64(a, b, r, c);
 }
 
+// The precision form's solve: A x = b in FP64 by the calling warp (all 32 lanes call),
+// a Cholesky factor formed column by column (pivot by lane j, its column by lanes
+// j+1..5, each entry's terms as FMAs in k order), the reciprocal pivots from the FP64
+// rsqrt, and both substitutions column-oriented so that each step is one FMA per lane.
+// A: 6x6 shared doubles, lower triangle on entry, the factor on return; x: 6 shared
+// doubles, b on entry, the solution on return when A is positive definite (else false
+// and x untouched).  r: 6 shared doubles of scratch.
+__device__ __forceinline__ bool warp_chol6_f64(double* A, double* x, double* r, int* fail)
+{
+    const int lane = threadIdx.x & 31;
+    if (lane == 0) *fail = 0;
+    __syncwarp();
+    for (int j = 0; j < 6; ++j) {
+        double s = 0.0;
+        if (lane >= j && lane < 6) {
+            s = A[lane * 6 + j];
+            for (int k = 0; k < j; ++k) s = fma(-A[lane * 6 + k], A[j * 6 + k], s);
+        }
+        if (lane == j) {
+            if (!(s > 0.0))
+                *fail = 1;
+            else {
+                const double q = rsqrt(s);
+                r[j] = q;
+                A[j * 6 + j] = s * q;
+            }
+        }
+        __syncwarp();
+        if (*fail) return false;
+        if (lane > j && lane < 6) A[lane * 6 + j] = s * r[j];
+        __syncwarp();
+    }
+    // forward: y_i = (b_i - sum_k L_ik y_k) / L_ii, lanes i > k subtract as y_k appears
+    double v = lane < 6 ? x[lane] : 0.0;
+    for (int k = 0; k < 6; ++k) {
+        if (lane == k) {
+            v = v * r[k];
+            x[k] = v;
+        }
+        __syncwarp();
+        if (lane > k && lane < 6) v = fma(-A[lane * 6 + k], x[k], v);
+    }
+    __syncwarp();
+    // backward: x_i = (y_i - sum_{k>i} L_ki x_k) / L_ii
+    v = lane < 6 ? x[lane] : 0.0;
+    for (int k = 5; k >= 0; --k) {
+        if (lane == k) {
+            v = v * r[k];
+            x[k] = v;
+        }
+        __syncwarp();
+        if (lane < k) v = fma(-A[k * 6 + lane], x[k], v);
+    }
+    __syncwarp();
+    return true;
+}
+
 }  // namespace kf

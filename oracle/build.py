@@ -4,7 +4,8 @@ Two shared libraries, both compiled with ``-ffp-contract=off`` so that every flo
 operation rounds where the source expression says (gcc on aarch64 would otherwise
 contract a*b+c into an FMA):
 
-* ``oracle/libkf_oracle.so`` -- the restatement in ``kf_oracle.cpp``.
+* ``oracle/libkf_oracle.so`` -- the restatement in ``kf_oracle.cpp`` and the FP64
+  oracle in ``kf_oracle64.cpp``.
 * ``oracle/_ref/libkf_ref.so`` -- the reference's own kernel bodies.  When the
   reference tree is available (``KF_REF_DIR``, default ``/root/reference``) this
   splices the kernel bodies out of its ``src/parallel_processing`` sources into
@@ -109,7 +110,7 @@ def _compile(out: Path, sources, extra=()) -> None:
 
 
 def build_oracle(force: bool = False) -> Path:
-    srcs = [HERE / "kf_oracle.cpp"]
+    srcs = [HERE / "kf_oracle.cpp", HERE / "kf_oracle64.cpp"]
     deps = srcs + [HERE / "kf_oracle.h", HERE / "ocv_restated.h"]
     if force or not _newer(ORACLE_SO, deps):
         _compile(ORACLE_SO, srcs)

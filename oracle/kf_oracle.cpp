@@ -469,6 +469,18 @@ int kfo_icp_associate(int H, int W, const float* K, const float* F, const float*
     return ncorr;
 }
 
+void kfo_icp_terms(int H, int W, const float* K, const float* F, const float* T, const float* cur6,
+                   const uint8_t* mask, const float* pred6, float* terms42)
+{
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < H * W; ++i) {
+        int32_t pidx = -1;
+        float t[42] = {};
+        icp_terms(H, W, i, K, F, T, cur6, mask, pred6, &pidx, t);
+        for (int k = 0; k < 42; ++k) terms42[(size_t)i * 42 + k] = t[k];
+    }
+}
+
 void kfo_estimate_pose(int H, int W, const float* K, float* T, const float* cur6, const uint8_t* mask,
                        const float* pred6, int iters, float* sums_log, float* pose_log, int32_t* ncorr_log,
                        int32_t* chol_ok_log)

@@ -67,6 +67,10 @@ int kfo_icp_associate(int H, int W, const float* K, const float* F, const float*
  * associate -> reference-order sums -> cv::Cholesky -> small-angle increment -> T <- Inc*T.
  * T is updated in place.  Optional logs: sums_log [iters][42], pose_log [iters][16],
  * ncorr_log [iters], chol_ok_log [iters]. */
+/* the per-pixel ICP products (6 a*b then 36 a*a, zero where the pixel is not a
+ * correspondence), H*W x 42 floats, for checking reductions */
+void kfo_icp_terms(int H, int W, const float* K, const float* F, const float* T, const float* cur6,
+                   const uint8_t* mask, const float* pred6, float* terms42);
 void kfo_estimate_pose(int H, int W, const float* K, float* T, const float* cur6, const uint8_t* mask,
                        const float* pred6, int iters, float* sums_log, float* pose_log,
                        int32_t* ncorr_log, int32_t* chol_ok_log);
@@ -96,6 +100,24 @@ void kfo_get_depth(const kfo_pipeline* p, float* depth);
 void kfo_get_vertex_map(const kfo_pipeline* p, float* cur6, uint8_t* mask);
 
 int kfo_num_threads(void);
+
+/* ---- the FP64 oracle (kf_oracle64.cpp): the same frame loop with every quantity in
+ * double and a double Cholesky solve; the yardstick of the precision form ---- */
+typedef struct kfo64_pipeline kfo64_pipeline;
+kfo64_pipeline* kfo64_create(int H, int W, double min_depth, double max_depth, const kfo_grid* g, const double* K,
+                             int icp_iters);
+void kfo64_destroy(kfo64_pipeline* p);
+void kfo64_initial(kfo64_pipeline* p, const uint16_t* raw);
+void kfo64_incoming(kfo64_pipeline* p, const uint16_t* raw);
+void kfo64_get_pose(const kfo64_pipeline* p, double* T);
+void kfo64_set_pose(kfo64_pipeline* p, const double* T);
+/* single stages at the current pose */
+void kfo64_integrate_frame(kfo64_pipeline* p, const uint16_t* raw, int first);
+void kfo64_raycast_frame(kfo64_pipeline* p);
+/* world-space predicted points and normals, 6 planes of H*W */
+void kfo64_get_prediction(const kfo64_pipeline* p, double* out6);
+/* the volume rounded to float, z-fastest reference order */
+void kfo64_get_volume(const kfo64_pipeline* p, float* tsdf, float* weight);
 
 #ifdef __cplusplus
 }

@@ -150,6 +150,19 @@ class Oracle(_Common):
         self._fn("kfo_get_depth", None, [C.c_void_p, _f32p])
         self._fn("kfo_get_vertex_map", None, [C.c_void_p, C.c_void_p, C.c_void_p])
         self._fn("kfo_num_threads", C.c_int, [])
+        self._fn("kfo_icp_terms", None, [C.c_int, C.c_int, _f32p, _f32p, _f32p, _f32p, _u8p, _f32p, _f32p])
+        _f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+        self._fn("kfo64_create", C.c_void_p, [C.c_int, C.c_int, C.c_double, C.c_double, C.POINTER(Grid), _f64p,
+                                               C.c_int])
+        self._fn("kfo64_destroy", None, [C.c_void_p])
+        self._fn("kfo64_initial", None, [C.c_void_p, _u16p])
+        self._fn("kfo64_incoming", None, [C.c_void_p, _u16p])
+        self._fn("kfo64_get_pose", None, [C.c_void_p, _f64p])
+        self._fn("kfo64_set_pose", None, [C.c_void_p, _f64p])
+        self._fn("kfo64_integrate_frame", None, [C.c_void_p, _u16p, C.c_int])
+        self._fn("kfo64_raycast_frame", None, [C.c_void_p])
+        self._fn("kfo64_get_prediction", None, [C.c_void_p, _f64p])
+        self._fn("kfo64_get_volume", None, [C.c_void_p, C.c_void_p, C.c_void_p])
         self.L = L
 
     def inv3(self, K):
@@ -190,8 +203,70 @@ class Oracle(_Common):
                                    iters, _nullable(sums), _nullable(poses), _nullable(ncorr), _nullable(ok))
         return T, {"sums": sums, "poses": poses.reshape(iters, 4, 4), "ncorr": ncorr, "chol_ok": ok}
 
+    def icp_terms(self, K, F, T, cur6, mask, pred6):
+        """(H*W, 42) per-pixel ICP products: a*b (6) then a a^T (36); zero off correspondences."""
+        _, H, W = cur6.shape
+        out = np.zeros((H * W, 42), np.float32)
+        self.lib.kfo_icp_terms(H, W, _c32(K), _c32(F), _c32(T), _c32(cur6), np.ascontiguousarray(mask, np.uint8),
+                               _c32(pred6), out)
+        return out
+
     def pipeline(self, H, W, grid: GridSpec, K, min_depth=300.0, max_depth=2000.0, icp_iters=10):
         return OraclePipeline(self, H, W, grid, K, min_depth, max_depth, icp_iters)
+
+    def pipeline64(self, H, W, grid: GridSpec, K, min_depth=300.0, max_depth=2000.0, icp_iters=10):
+        """The FP64 oracle's frame loop (kf_oracle64.cpp)."""
+        return Oracle64Pipeline(self, H, W, grid, K, min_depth, max_depth, icp_iters)
+
+
+class Oracle64Pipeline:
+    """The frame loop with every quantity in double (the precision form's yardstick)."""
+
+    def __init__(self, o: Oracle, H, W, grid: GridSpec, K, min_depth, max_depth, icp_iters):
+        self.o, self.H, self.W, self.grid = o, H, W, grid
+        self._g = grid.c()
+        K64 = np.ascontiguousarray(np.asarray(K, np.float32).astype(np.float64).ravel())
+        self.h = o.lib.kfo64_create(H, W, min_depth, max_depth, C.byref(self._g), K64, icp_iters)
+
+    def close(self):
+        if self.h:
+            self.o.lib.kfo64_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    def initial(self, raw):
+        self.o.lib.kfo64_initial(self.h, np.ascontiguousarray(raw, np.uint16).ravel())
+
+    def incoming(self, raw):
+        self.o.lib.kfo64_incoming(self.h, np.ascontiguousarray(raw, np.uint16).ravel())
+
+    @property
+    def pose(self):
+        T = np.zeros(16, np.float64)
+        self.o.lib.kfo64_get_pose(self.h, T)
+        return T.reshape(4, 4)
+
+    @pose.setter
+    def pose(self, T):
+        self.o.lib.kfo64_set_pose(self.h, np.ascontiguousarray(T, np.float64).ravel())
+
+    def integrate_frame(self, raw, first: bool):
+        self.o.lib.kfo64_integrate_frame(self.h, np.ascontiguousarray(raw, np.uint16).ravel(), int(first))
+
+    def raycast_frame(self):
+        self.o.lib.kfo64_raycast_frame(self.h)
+
+    def prediction(self):
+        out6 = np.zeros((6, self.H, self.W), np.float64)
+        self.o.lib.kfo64_get_prediction(self.h, out6)
+        return out6
+
+    def volume(self):
+        t = np.zeros(self.grid.nvox, np.float32)
+        w = np.zeros(self.grid.nvox, np.float32)
+        self.o.lib.kfo64_get_volume(self.h, _nullable(t), _nullable(w))
+        return t, w
 
 
 class OraclePipeline:

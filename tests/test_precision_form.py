@@ -1,0 +1,172 @@
+"""The precision form against the FP64 oracle.
+
+The precision form stores the TSDF as an FP16 value + FP16 weight pair, keeps the
+association and the per-pixel Jacobians in FP32, adds the normal-equation sums with
+compensated (TwoSum) FP32 and solves and composes the pose in FP64.  It is held to the
+FP64 oracle (oracle/kf_oracle64.cpp: the same algorithm in double), stage by stage:
+
+* the TSDF and weights after integrating frames at fixed poses (open loop),
+* the predicted surface after a ray cast at a fixed pose,
+* the 27 normal-equation sums of one ICP association, against the exact sum of the
+  oracle's per-pixel products,
+* the pose after one tracked frame.
+
+Closed-loop trajectories are not compared here: the reference's tracker amplifies
+differences in the last bit into millimetres within a few frames (its own float
+arithmetic is 22 mm ATE from the FP64 run over the first 48 frames of the benchmark
+sequence), so the benchmark reports those numbers rather than gating on them.
+"""
+import numpy as np
+import pytest
+
+import kinect_fusion_slam_gb300 as kf
+from conftest import grid_spec
+
+pytestmark = pytest.mark.gpu
+
+
+def _precise_handle(seq, H, W):
+    g = seq.cfg.grid
+    h = kf.Handle(kf.make_config(height=H, width=W, dims=g.dims, grid_start=g.start, voxel_size=g.voxel_size,
+                                 tsdf_storage=kf.KF_TSDF_F16, solve_mode=kf.KF_SOLVE_PRECISE,
+                                 icp_reduction=kf.KF_REDUCE_TREE))
+    K = seq.K
+    h.set_intrinsics(K[0, 0], K[1, 1], K[0, 2], K[1, 2])
+    return h
+
+
+def _integrate_open_loop(oracle, seq, depths, frames):
+    """The same frames integrated at the same float poses by the precision form, the
+    FP64 oracle and the float oracle (the reference's own arithmetic)."""
+    H, W = depths.shape[1:]
+    h = _precise_handle(seq, H, W)
+    gs = grid_spec(seq.cfg.grid)
+    p64 = oracle.pipeline64(H, W, gs, seq.K)
+    K = seq.K
+    Ki = oracle.inv3(K)
+    t32 = np.full(gs.nvox, np.nan, np.float32)
+    w32 = np.full(gs.nvox, np.nan, np.float32)
+    for n, k in enumerate(frames):
+        T = seq.poses[k].astype(np.float32)
+        h.set_pose(T)
+        h.set_depth_u16(depths[k])
+        h.projective_tsdf(first=(n == 0))
+        p64.pose = T.astype(np.float64)
+        p64.integrate_frame(depths[k], n == 0)
+        oracle.integrate(gs, oracle.depth_ingest(depths[k]), K, Ki, T, oracle.inv4(T), t32, w32, first=(n == 0))
+    return h, p64, (t32, w32)
+
+
+def test_fp16_tsdf_against_fp64_oracle(oracle, small_seq):
+    seq, depths = small_seq
+    h, p64, (t32, w32) = _integrate_open_loop(oracle, seq, depths, [0, 1, 2, 3])
+    t16, w16 = h.volume()
+    t64, w64 = p64.volume()
+    o16, o64 = ~np.isnan(w16), ~np.isnan(w64)
+    both = o16 & o64
+    assert both.sum() > 10000
+    # projections that round differently in float and double flip a few voxels in or out
+    assert (o16 ^ o64).sum() <= 0.01 * both.sum()
+    same_w = both & (w16 == w64) & (w32 == w64)
+    assert same_w.sum() >= 0.99 * both.sum()
+    # the float pipeline's own distance from FP64 (a depth sample taken from the
+    # neighbouring pixel where a projection rounds the other way) plus FP16's 11
+    # significant bits through four running-average updates (< 1.5e-3)
+    err16 = np.abs(t16[same_w] - t64[same_w])
+    err32 = np.abs(t32[same_w] - t64[same_w])
+    q16, q32 = np.quantile(err16, 0.999), np.quantile(err32, 0.999)
+    assert q16 <= q32 + 1.5e-3, (q16, q32)
+    assert np.mean(err16) <= np.mean(err32) + 3e-4, (np.mean(err16), np.mean(err32))
+
+
+def test_fp16_prediction_against_fp64_oracle(oracle, small_seq):
+    seq, depths = small_seq
+    h, p64, _ = _integrate_open_loop(oracle, seq, depths, [0, 1, 2])
+    h.ray_casting()
+    pred16 = h.predicted().astype(np.float64)
+    p64.raycast_frame()
+    pred64 = p64.prediction()
+    hit16, hit64 = pred16[2] != 0, pred64[2] != 0
+    both = hit16 & hit64
+    assert both.sum() > 1000
+    assert (hit16 ^ hit64).sum() <= 0.05 * both.sum()
+    d = np.linalg.norm(pred16[:3, both] - pred64[:3, both], axis=0)
+    # 20 mm voxels, TSDF normalised by 300 mm: FP16 rounding moves the zero crossing by
+    # well under a millimetre
+    assert np.median(d) <= 0.5, np.median(d)
+    assert np.percentile(d, 95) <= 3.0, np.percentile(d, 95)
+
+
+def _tri(r, s):
+    return 6 + r * 6 - r * (r - 1) // 2 + (s - r)
+
+
+def test_compensated_sums_against_exact_sum(oracle, small_seq):
+    """One association at a perturbed pose: the compensated FP32 sums agree with the
+    exact (float64) sum of the oracle's per-pixel products to ~1e-7 relative."""
+    seq, depths = small_seq
+    H, W = depths.shape[1:]
+    K = seq.K
+    Ki = oracle.inv3(K)
+    gs = grid_spec(seq.cfg.grid)
+    t = np.full(gs.nvox, np.nan, np.float32)
+    w = np.full(gs.nvox, np.nan, np.float32)
+    T0 = seq.poses[0].astype(np.float32)
+    d0 = oracle.depth_ingest(depths[0])
+    oracle.integrate(gs, d0, K, Ki, T0, oracle.inv4(T0), t, w, first=True)
+    pred6, _ = oracle.raycast(gs, d0, Ki, T0, t)
+    d1 = oracle.depth_ingest(depths[1])
+    v5, mask = oracle.vertex_normal(d1, Ki)
+    cur6 = np.stack([v5[0], v5[1], d1, v5[2], v5[3], v5[4]])
+    T = T0.copy()
+    T[:3, 3] += np.float32(3.0)
+    F = oracle.matmul4(oracle.inv4(T0), T)
+    terms = oracle.icp_terms(K, F, T, cur6, mask, pred6).astype(np.float64)
+    exact = np.zeros(27)
+    exact[:6] = terms[:, :6].sum(0)
+    for r in range(6):
+        for s in range(r, 6):
+            exact[_tri(r, s)] = terms[:, 6 + r * 6 + s].sum()
+
+    h = _precise_handle(seq, H, W)
+    h.set_depth_f32(d1)
+    h.calculate_vertices_and_normals()
+    h.set_predicted(pred6)
+    n, sums, _ = h.icp_associate(F, T)
+    n_ref, _, _ = oracle.icp_associate(K, F, T, cur6, mask, pred6)
+    assert n == n_ref and n > 200  # the association is the plain form's, bit for bit
+    scale = np.abs(terms).sum(0)
+    mags = np.zeros(27)
+    mags[:6] = scale[:6]
+    for r in range(6):
+        for s in range(r, 6):
+            mags[_tri(r, s)] = scale[6 + r * 6 + s]
+    rel = np.abs(sums.astype(np.float64) - exact) / np.maximum(mags, 1e-30)
+    assert rel.max() <= 2e-6, rel.max()
+
+
+def _pose_gap(Ta, Tb):
+    R = Ta[:3, :3].T @ Tb[:3, :3]
+    return (float(np.linalg.norm(Ta[:3, 3] - Tb[:3, 3])),
+            float(np.degrees(np.arccos(np.clip((np.trace(R) - 1) / 2, -1, 1)))))
+
+
+def test_one_tracked_frame_against_fp64_oracle(oracle, small_seq):
+    """After one tracked frame the precision form is no further from the FP64 run than
+    the reference's float arithmetic is (that sensitivity is the tracker's, not the
+    storage's), within a millimetre and a tenth of a degree."""
+    seq, depths = small_seq
+    H, W = depths.shape[1:]
+    h = _precise_handle(seq, H, W)
+    gs = grid_spec(seq.cfg.grid)
+    p64 = oracle.pipeline64(H, W, gs, seq.K)
+    p32 = oracle.pipeline(H, W, gs, seq.K)
+    for p in (h, p64, p32):
+        (p.initial_processing if p is h else p.initial)(depths[0])
+        (p.incoming_frame if p is h else p.incoming)(depths[1])
+    nc, ok = h.icp_stats(10)
+    assert nc[-1] > 100
+    dt16, ang16 = _pose_gap(h.pose().astype(np.float64), p64.pose)
+    dt32, ang32 = _pose_gap(p32.pose.astype(np.float64), p64.pose)
+    assert dt16 <= 2 * dt32 + 1.0, (dt16, dt32)
+    assert ang16 <= 2 * ang32 + 0.1, (ang16, ang32)
