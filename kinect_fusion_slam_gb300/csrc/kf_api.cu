@@ -924,11 +924,11 @@ kf_status kf_get_stage_times(kf_handle* h, float ms[5])
 kf_status kf_kernels_per_frame(kf_handle* h, int* n)
 {
     if (!h || !n) return KF_ERR_INVALID_ARGUMENT;
-    // vertex, [bilateral], ICP iterations (a 64-pixel group pass, then the reduce-and-solve
-    // pass, in the reference summation order or compensated for the FP64 solve; the
-    // one-pass tree is a single kernel), integration prep, integration, ray cast
+    // vertex, [bilateral], ICP iterations (in the reference summation order a 64-pixel
+    // group pass and a one-warp reduce-and-solve pass; the precision form and the tree
+    // reduction one pass each), integration prep, integration, ray cast
     const int per_iteration =
-        (h->cfg.icp_reduction == KF_REDUCE_REFERENCE_ORDER || h->cfg.solve_mode == KF_SOLVE_PRECISE) ? 2 : 1;
+        (h->cfg.icp_reduction == KF_REDUCE_REFERENCE_ORDER && h->cfg.solve_mode != KF_SOLVE_PRECISE) ? 2 : 1;
     *n = 1 + (h->cfg.bilateral ? 1 : 0) + per_iteration * h->cfg.icp_iterations[0] + 3;
     return KF_OK;
 }

@@ -217,9 +217,17 @@ __device__ void finish_precise_warp(State* st, const IcpParams& prm, const float
         Tp[lane] = st->Tprev_inv[lane];
         Tn[lane] = st->Td[lane];
     }
-    if (lane < 6) {
-        x[lane] = (double)hi[lane] + (double)lo[lane];
-        for (int c = 0; c <= lane; ++c) A[lane * 6 + c] = (double)hi[tri(c, lane)] + (double)lo[tri(c, lane)];
+    // one sum per lane: b (lanes 0..5) or an entry of A's lower triangle (lanes 6..26)
+    if (lane < kIcpVals - 1) {
+        const double val = (double)hi[lane] + (double)lo[lane];
+        if (lane < 6) {
+            x[lane] = val;
+        } else {
+            int r = 0;
+            while (r < 5 && lane >= tri(r + 1, r + 1)) ++r;
+            const int c = r + (lane - tri(r, r));  // sums index tri(r, c), c >= r
+            A[c * 6 + r] = val;
+        }
     }
     if (lane < kIcpVals) st->sums[lane] = hi[lane] + lo[lane];
     __syncwarp();
@@ -586,51 +594,146 @@ __global__ void __launch_bounds__(32, 1) icp_solve_kernel(const float* __restric
     finish_iteration_warp(st, prm, red, sT0, sTp, it);
 }
 
-// The precision form's reduce-and-solve pass: one block of 32 warps.  The group sums
-// of the group pass are added with compensated (TwoSum) FP32 arithmetic -- warp w,
-// lane k accumulates term k over groups w, w + 32, ...; the 32 warp partials are then
-// combined the same way -- and warp 0 solves in FP64 (finish_precise_warp, MODE 0) or
-// writes hi + lo (MODE 1).  Summation order is free here: the precision form is held
-// to the FP64 oracle, not to the reference's bits.
-constexpr int kPreciseWarps = 32;
+// The precision form in one pass per iteration.  One warp per 64-pixel group forms the
+// group's 28 sums (as in the group pass); the block combines its groups with
+// compensated (TwoSum) FP32 and writes one hi/lo partial.  The blocks are then reduced
+// in two levels: the last block of each slab of consecutive blocks (a ticket per slab)
+// adds the slab's partials, and the last slab to finish adds the slab partials and
+// solves in FP64 (finish_precise_warp, MODE 0) or writes hi + lo (MODE 1).  A level
+// issues all its loads before adding, so its latency is about one trip to L2.
+// Summation order is free here: the precision form is held to the FP64 oracle, not to
+// the reference's bits.
+constexpr int kSlabRows = 32;
+
+// Adds nrows rows of [hi(28) | lo(28)] with compensation into red_hi/red_lo (shared).
+// Four threads per column take every fourth row; all threads of the block call.
+__device__ __forceinline__ void reduce_rows(const float* rows, int nrows, float* red_hi, float* red_lo)
+{
+    constexpr int kCols = 2 * kIcpVals;
+    constexpr int kLanes = (kExactWarps * 32) / kCols;
+    __shared__ float ph[kLanes][kIcpVals], pc[kLanes][kIcpVals], pl[kLanes][kIcpVals];
+    const int t = threadIdx.x;
+    if (t < kLanes * kCols) {
+        const int col = t % kCols, r0 = t / kCols;
+        float h = 0.f, l = 0.f;
+        for (int base = r0; base < nrows; base += kLanes * 8) {
+            float v[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const int r = base + u * kLanes;
+                v[u] = r < nrows ? __ldcg(rows + (size_t)r * kCols + col) : 0.f;
+            }
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                float sum, e;
+                two_sum(h, v[u], sum, e);
+                h = sum;
+                l += e;
+            }
+        }
+        if (col < kIcpVals) {
+            ph[r0][col] = h;
+            pc[r0][col] = l;
+        } else {
+            pl[r0][col - kIcpVals] = h + l;
+        }
+    }
+    __syncthreads();
+    if (t < kIcpVals) {
+        float H = 0.f, L = 0.f;
+        for (int q = 0; q < kLanes; ++q) {
+            float sum, e;
+            two_sum(H, ph[q][t], sum, e);
+            H = sum;
+            L += (e + pc[q][t]) + pl[q][t];
+        }
+        red_hi[t] = H;
+        red_lo[t] = L;
+    }
+    __syncthreads();
+}
 
 template <int MODE>
-__global__ void __launch_bounds__(kPreciseWarps * 32, 1) icp_precise_reduce_kernel(
-    const float* __restrict__ partials, int ngroups, State* st, IcpParams prm, float* sums_out)
+__global__ void __launch_bounds__(kExactWarps * 32, 4) icp_precise_kernel(
+    const float4* __restrict__ vmap, const float4* __restrict__ nmap, const float4* __restrict__ pv,
+    const float4* __restrict__ pn, Camera cam, IcpParams prm, const float* Fsrc, const float* Tsrc, State* st,
+    float* __restrict__ partials, int ngroups, int32_t* __restrict__ pair, float* sums_out)
 {
     wait_for_producer();
-    __shared__ float sh_hi[kPreciseWarps][kIcpVals], sh_lo[kPreciseWarps][kIcpVals];
+    __shared__ float sF[16], sT[16];
+    __shared__ float wsum[kExactWarps][kIcpVals];
     __shared__ float red_hi[kIcpVals], red_lo[kIcpVals];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int term = lane < kIcpVals ? lane : kIcpVals - 1;
-    float h = 0.f, l = 0.f;
-#pragma unroll 8
-    for (int g = warp; g < ngroups; g += kPreciseWarps) {
-        const float v = __ldcg(partials + (size_t)g * kIcpVals + term);
-        float sum, e;
-        two_sum(h, v, sum, e);
-        h = sum;
-        l += e;
-    }
-    if (lane < kIcpVals) {
-        sh_hi[warp][lane] = h;
-        sh_lo[warp][lane] = l;
+    __shared__ int is_last;
+    if (threadIdx.x < 16) {
+        sF[threadIdx.x] = Fsrc[threadIdx.x];
+        sT[threadIdx.x] = Tsrc[threadIdx.x];
     }
     __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int n = cam.H * cam.W;
+    const int grp = blockIdx.x * kExactWarps + warp;
+    float v[kIcpVals];
+#pragma unroll
+    for (int k = 0; k < kIcpVals; ++k) v[k] = 0.f;
+    if (grp < ngroups) {
+        for (int half = 0; half < 2; ++half) {
+            const int i = grp * 64 + half * 32 + lane;
+            if (i >= n) continue;
+            float a[6], b;
+            int j = -1;
+            const bool ok = associate(i, vmap, nmap, pv, pn, cam, sF, sT, prm.dist, prm.angle_deg, a, b, j);
+            if (MODE == 1 && pair) pair[i] = ok ? j : -1;
+            if (ok) add_terms(v, a, b);
+        }
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1)
+#pragma unroll
+            for (int k = 0; k < kIcpVals; ++k) v[k] = v[k] + __shfl_xor_sync(0xffffffffu, v[k], off);
+    }
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < kIcpVals; ++k) wsum[warp][k] = v[k];
+    __syncthreads();
+    const int nblocks = gridDim.x;
     if (threadIdx.x < kIcpVals) {
         const int k = threadIdx.x;
-        float H = sh_hi[0][k], L = sh_lo[0][k];
-        for (int w = 1; w < kPreciseWarps; ++w) {
+        float h = wsum[0][k], l = 0.f;
+        for (int w = 1; w < kExactWarps; ++w) {
             float sum, e;
-            two_sum(H, sh_hi[w][k], sum, e);
-            H = sum;
-            L += e + sh_lo[w][k];
+            two_sum(h, wsum[w][k], sum, e);
+            h = sum;
+            l += e;
         }
-        red_hi[k] = H;
-        red_lo[k] = L;
+        partials[(size_t)blockIdx.x * 2 * kIcpVals + k] = h;
+        partials[(size_t)blockIdx.x * 2 * kIcpVals + kIcpVals + k] = l;
+        __threadfence();
     }
+    // level 1: the slab's last block adds the slab's block partials
+    const int slab_size = max(kSlabRows, (nblocks + kMaxSlabs - 1) / kMaxSlabs);
+    const int slab = blockIdx.x / slab_size, nslabs = (nblocks + slab_size - 1) / slab_size;
+    const int slab_lo = slab * slab_size, slab_n = min(slab_size, nblocks - slab_lo);
     __syncthreads();
-    if (warp != 0) return;
+    if (threadIdx.x == 0) is_last = atomicAdd(&st->slab_ticket[slab], 1u) == (unsigned)slab_n - 1;
+    __syncthreads();
+    if (!is_last) return;
+    __threadfence();
+    reduce_rows(partials + (size_t)slab_lo * 2 * kIcpVals, slab_n, red_hi, red_lo);
+    float* slab_part = partials + (size_t)nblocks * 2 * kIcpVals;
+    if (threadIdx.x < kIcpVals) {
+        slab_part[(size_t)slab * 2 * kIcpVals + threadIdx.x] = red_hi[threadIdx.x];
+        slab_part[(size_t)slab * 2 * kIcpVals + kIcpVals + threadIdx.x] = red_lo[threadIdx.x];
+        __threadfence();
+    }
+    if (threadIdx.x == 0) st->slab_ticket[slab] = 0u;
+    __syncthreads();
+    // level 2: the last slab adds the slab partials and finishes the iteration
+    if (threadIdx.x == 0) is_last = atomicAdd(&st->ticket, 1u) == (unsigned)nslabs - 1;
+    __syncthreads();
+    if (!is_last) return;
+    __threadfence();
+    reduce_rows(slab_part, nslabs, red_hi, red_lo);
+    if (threadIdx.x == 0) st->ticket = 0u;
+    if (threadIdx.x >= 32) return;
     if (MODE == 1) {
         if (lane < kIcpVals) sums_out[lane] = red_hi[lane] + red_lo[lane];
         return;
@@ -675,7 +778,9 @@ size_t icp_scratch_floats(int H, int W)
 {
     const size_t a = (size_t)2 * blocks_for(H, W) * kIcpVals;
     const size_t b = (size_t)icp_groups(H, W) * kIcpVals;
-    return a > b ? a : b;
+    // the precision form: block partials then slab partials, hi/lo each
+    const size_t c = (size_t)2 * kIcpVals * ((icp_groups(H, W) + kExactWarps - 1) / kExactWarps + kMaxSlabs);
+    return a > b ? (a > c ? a : c) : (b > c ? b : c);
 }
 
 namespace {
@@ -700,10 +805,8 @@ void launch_icp_iteration(const float4* vmap, const float4* nmap, const float4* 
                    prm, (float*)nullptr);
     } else if (prm.precise) {
         const int ng = icp_groups(cam.H, cam.W);
-        launch_pdl(icp_group_kernel<0>, dim3(exact_blocks(cam.H, cam.W)), dim3(kExactWarps * 32), 0, s, vmap, nmap, pv,
-                   pn, cam, prm, state_F(st), state_T(st), partials, list, ng, (int32_t*)nullptr);
-        launch_pdl(icp_precise_reduce_kernel<0>, dim3(1), dim3(kPreciseWarps * 32), 0, s, (const float*)partials, ng,
-                   st, prm, (float*)nullptr);
+        launch_pdl(icp_precise_kernel<0>, dim3(exact_blocks(cam.H, cam.W)), dim3(kExactWarps * 32), 0, s, vmap, nmap,
+                   pv, pn, cam, prm, state_F(st), state_T(st), st, partials, ng, (int32_t*)nullptr, (float*)nullptr);
     } else
         icp_kernel<false, 0><<<blocks, kIcpBlock, 0, s>>>(vmap, nmap, pv, pn, cam, prm, st, state_F(st),
                                                           state_T(st), partials, nullptr, nullptr);
@@ -723,10 +826,8 @@ void launch_icp_associate(const float4* vmap, const float4* nmap, const float4* 
                    prm, sums_out);
     } else if (prm.precise) {
         const int ng = icp_groups(cam.H, cam.W);
-        launch_pdl(icp_group_kernel<1>, dim3(exact_blocks(cam.H, cam.W)), dim3(kExactWarps * 32), 0, s, vmap, nmap, pv,
-                   pn, cam, prm, F, T, partials, list, ng, pair);
-        launch_pdl(icp_precise_reduce_kernel<1>, dim3(1), dim3(kPreciseWarps * 32), 0, s, (const float*)partials, ng,
-                   st, prm, sums_out);
+        launch_pdl(icp_precise_kernel<1>, dim3(exact_blocks(cam.H, cam.W)), dim3(kExactWarps * 32), 0, s, vmap, nmap,
+                   pv, pn, cam, prm, F, T, st, partials, ng, pair, sums_out);
     } else
         icp_kernel<false, 1><<<blocks, kIcpBlock, 0, s>>>(vmap, nmap, pv, pn, cam, prm, st, F, T, partials,
                                                           sums_out, pair);

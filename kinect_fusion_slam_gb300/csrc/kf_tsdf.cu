@@ -42,14 +42,25 @@ struct VolF16 {
     __device__ __forceinline__ void store(int i, float tv, float wv) const { p[i] = __floats2half2_rn(tv, wv); }
 };
 
+// Read-only views for the ray cast.  raw() loads a voxel without converting it, so a
+// prefetched load is not waited for until decode() at its use.
 struct ViewF32 {
+    using Raw = float;
     const float* t;
     __device__ __forceinline__ float value(int i) const { return __ldg(t + i); }
+    __device__ __forceinline__ Raw raw(int i) const { return __ldg(t + i); }
+    __device__ static __forceinline__ float decode(Raw r) { return r; }
 };
 
 struct ViewF16 {
+    using Raw = unsigned;  // the (value, weight) pair's bits; the value is the low half
     const __half2* p;
     __device__ __forceinline__ float value(int i) const { return __half2float(__low2half(__ldg(p + i))); }
+    __device__ __forceinline__ Raw raw(int i) const { return __ldg(reinterpret_cast<const unsigned*>(p) + i); }
+    __device__ static __forceinline__ float decode(Raw r)
+    {
+        return __half2float(__ushort_as_half((unsigned short)(r & 0xffffu)));
+    }
 };
 
 // Per pixel (u, v) (1-based): the quantities of projective_tsdf.cu:39-95 that depend
@@ -350,10 +361,10 @@ __device__ __forceinline__ void trace(const View& vol, float X, float Y, float D
         atm.y = by ? ny : atm.y;
         atm.z = bz ? nz : atm.z;
     };
-    float ring[kAhead];
+    typename View::Raw ring[kAhead];
 #pragma unroll
     for (int k = 0; k < kAhead; ++k) {
-        ring[k] = inside_grid(ax, ay, az) ? vol.value(ali) : 0.f;
+        ring[k] = inside_grid(ax, ay, az) ? vol.raw(ali) : typename View::Raw(0);
         lead_step();
     }
     float prev = 0.0f;
@@ -368,8 +379,8 @@ __device__ __forceinline__ void trace(const View& vol, float X, float Y, float D
                 done = true;
                 break;
             }
-            const float cur = ring[k];
-            ring[k] = inside_grid(ax, ay, az) ? vol.value(ali) : 0.f;
+            const float cur = View::decode(ring[k]);
+            ring[k] = inside_grid(ax, ay, az) ? vol.raw(ali) : typename View::Raw(0);
             lead_step();
             // the reference's four tests (:207-222) are mutually exclusive in prev
             const bool stop = prev < 0.f ? !(cur <= 0.f) : (isnan(prev) && cur < 0.f);
