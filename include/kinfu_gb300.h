@@ -197,6 +197,23 @@ kf_status kf_icp_associate_noalloc(int height, int width, const float K[9], cons
                                    const float* vmap, const float* nmap, const float* pred_v, const float* pred_n,
                                    float dist_mm, float angle_deg, float* sums28, int32_t* pair, void* stream);
 
+/* ---- export and checkpoint ------------------------------------------------------
+ * kf_export_ply: the latest ray cast's predicted surface as a binary little-endian
+ * PLY point cloud (x y z nx ny nz in mm, world frame, red green blue), headless in
+ * place of ThreeDViewer::SetUpPointClouds (threeD_viewer.cpp:20-54): a point per pixel
+ * whose surface_prediction_z != 0, in pixel order.  colour_bgr: the H*W*3 uint8 BGR
+ * image the viewer colours with (system_utility's color_image), host, or NULL to
+ * colour each point by its normal.  n_points (may be NULL) receives the point count.
+ * Synchronous. */
+kf_status kf_export_ply(kf_handle* h, const char* path, const uint8_t* colour_bgr, int* n_points);
+/* kf_save_checkpoint / kf_load_checkpoint: the volume, the pose (float and FP64), the
+ * intrinsics and the latest prediction, to and from a file, so a run resumes with
+ * kf_incoming_frame.  The reference has no counterpart.  Loading needs a handle of the
+ * same image size, grid (dims, start, voxel size, truncation) and TSDF storage, else
+ * KF_ERR_INVALID_ARGUMENT; a damaged or foreign file gives KF_ERR_IO.  Synchronous. */
+kf_status kf_save_checkpoint(kf_handle* h, const char* path);
+kf_status kf_load_checkpoint(kf_handle* h, const char* path);
+
 /* ---- timing --------------------------------------------------------------------- */
 /* per-stage device time of the latest kf_incoming_frame (CUDA events, ms):
  * [0] depth+vertex, [1] ICP, [2] integration, [3] ray cast, [4] whole frame.
@@ -205,6 +222,16 @@ kf_status kf_enable_stage_timing(kf_handle* h, int enable);
 kf_status kf_get_stage_times(kf_handle* h, float ms[5]);
 /* number of kernels one kf_incoming_frame launches */
 kf_status kf_kernels_per_frame(kf_handle* h, int* n);
+
+/* ---- diagnostics (no counterpart in the reference) --------------------------------
+ * The ICP pose update computes cv::Cholesky's and cv::Mat's double-accumulated results
+ * in float-float arithmetic with an exact FP64 fallback.  This runs that code and its
+ * FP64 restatement on seeded random 6x6 systems and 4x4 products (blocks x 4 warps x
+ * systems_per_warp of each) on the current device and counts: [0] systems, [1] solves
+ * that differ in any bit, [2] differing factorisation outcomes, [3] systems that are
+ * not positive definite, [4] differing product entries.  Synchronous. */
+kf_status kf_selftest_solve(unsigned long long seed, int blocks, int systems_per_warp,
+                            unsigned long long counts[5]);
 
 #ifdef __cplusplus
 }

@@ -151,6 +151,24 @@ class Handle:
         self._check(self.lib.kf_get_predicted(self.h, *[_lib.ptr(out[k]) for k in range(6)]))
         return out
 
+    def export_ply(self, path, colour_bgr=None) -> int:
+        """Write the latest predicted surface as a binary PLY (the viewer's point cloud);
+        colour_bgr: optional (H, W, 3) uint8 BGR image.  Returns the point count."""
+        n = C.c_int(0)
+        col = None
+        if colour_bgr is not None:
+            col = np.ascontiguousarray(colour_bgr, np.uint8)
+            if col.shape != (self.H, self.W, 3):
+                raise ValueError(f"colour image must be ({self.H}, {self.W}, 3)")
+        self._check(self.lib.kf_export_ply(self.h, str(path).encode(), _lib.ptr(col), C.byref(n)))
+        return int(n.value)
+
+    def save_checkpoint(self, path) -> None:
+        self._check(self.lib.kf_save_checkpoint(self.h, str(path).encode()))
+
+    def load_checkpoint(self, path) -> None:
+        self._check(self.lib.kf_load_checkpoint(self.h, str(path).encode()))
+
     def set_predicted(self, pred6) -> None:
         p = _f32(pred6).reshape(6, self.H, self.W)
         self._check(self.lib.kf_set_predicted(self.h, *[np.ascontiguousarray(p[k]).ravel() for k in range(6)]))

@@ -113,6 +113,10 @@ SIGNATURES = {
     "kf_enable_stage_timing": (C.c_int, [_H, C.c_int]),
     "kf_get_stage_times": (C.c_int, [_H, _f32p]),
     "kf_kernels_per_frame": (C.c_int, [_H, C.POINTER(C.c_int)]),
+    "kf_export_ply": (C.c_int, [_H, C.c_char_p, C.c_void_p, C.POINTER(C.c_int)]),
+    "kf_save_checkpoint": (C.c_int, [_H, C.c_char_p]),
+    "kf_load_checkpoint": (C.c_int, [_H, C.c_char_p]),
+    "kf_selftest_solve": (C.c_int, [C.c_ulonglong, C.c_int, C.c_int, C.POINTER(C.c_ulonglong)]),
     "kf_icp_associate_noalloc": (C.c_int, [C.c_int, C.c_int, _f32p, _f32p, _f32p, _vp, _vp, _vp, _vp, C.c_float,
                                            C.c_float, _vp, _vp, _vp]),
 }

@@ -5,6 +5,7 @@
 // CUDA stream and, optionally, the per-frame kernel sequence captured as CUDA graphs.
 // The pose never leaves the device during a frame: every kernel reads it from, and
 // the ICP's last block writes it to, the State block.
+#include <algorithm>
 #include <cmath>
 #include <cstddef>
 #include <cstdio>
@@ -744,6 +745,205 @@ kf_status kf_set_volume(kf_handle* h, const float* tsdf, const float* weight)
     cudaFree(dt);
     cudaFree(dw);
     if (e != cudaSuccess) return fail(h, KF_ERR_CUDA, std::string("kf_set_volume: ") + cudaGetErrorString(e));
+    return KF_OK;
+}
+
+kf_status kf_export_ply(kf_handle* h, const char* path, const uint8_t* colour_bgr, int* n_points)
+{
+    KF_HANDLE(h);
+    if (!path) return fail(h, KF_ERR_INVALID_ARGUMENT, "null path");
+    const int n = h->cam.H * h->cam.W;
+    float4* d_cloud = nullptr;
+    unsigned* d_count = nullptr;
+    KF_CUDA(h, cudaMalloc((void**)&d_cloud, sizeof(float4) * 2 * (size_t)n + sizeof(unsigned)));
+    d_count = reinterpret_cast<unsigned*>(d_cloud + 2 * (size_t)n);
+    cudaError_t e = cudaMemsetAsync(d_count, 0, sizeof(unsigned), h->stream);
+    if (e == cudaSuccess) {
+        launch_compact_cloud(h->d_pv, h->d_pn, n, d_cloud, d_count, h->stream);
+        e = cudaGetLastError();
+    }
+    unsigned count = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&count, d_count, sizeof(unsigned), cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    std::vector<float4> cloud(2 * (size_t)count);
+    if (e == cudaSuccess && count)
+        e = cudaMemcpy(cloud.data(), d_cloud, sizeof(float4) * cloud.size(), cudaMemcpyDeviceToHost);
+    cudaFree(d_cloud);
+    if (e != cudaSuccess) return fail(h, KF_ERR_CUDA, std::string("kf_export_ply: ") + cudaGetErrorString(e));
+    // pixel order, as the viewer fills its cloud
+    std::vector<unsigned> order(count);
+    for (unsigned k = 0; k < count; ++k) order[k] = k;
+    std::sort(order.begin(), order.end(), [&](unsigned a, unsigned b) {
+        return __builtin_bit_cast(int, cloud[2 * a].w) < __builtin_bit_cast(int, cloud[2 * b].w);
+    });
+    FILE* f = std::fopen(path, "wb");
+    if (!f) return fail(h, KF_ERR_IO, std::string("cannot open ") + path);
+    std::fprintf(f,
+                 "ply\nformat binary_little_endian 1.0\ncomment kinfu_gb300 predicted surface, mm, world frame\n"
+                 "element vertex %u\nproperty float x\nproperty float y\nproperty float z\nproperty float nx\n"
+                 "property float ny\nproperty float nz\nproperty uchar red\nproperty uchar green\n"
+                 "property uchar blue\nend_header\n",
+                 count);
+    bool ok = true;
+    for (unsigned k = 0; k < count && ok; ++k) {
+        const float4 p = cloud[2 * order[k]], q = cloud[2 * order[k] + 1];
+        const int pix = __builtin_bit_cast(int, p.w);
+        unsigned char rgb[3];
+        if (colour_bgr) {
+            rgb[0] = colour_bgr[3 * (size_t)pix + 2];
+            rgb[1] = colour_bgr[3 * (size_t)pix + 1];
+            rgb[2] = colour_bgr[3 * (size_t)pix];
+        } else {
+            const float c[3] = {q.x, q.y, q.z};
+            for (int j = 0; j < 3; ++j) {
+                const float v = std::isfinite(c[j]) ? 127.5f * (c[j] + 1.f) : 0.f;
+                rgb[j] = (unsigned char)(v < 0.f ? 0.f : (v > 255.f ? 255.f : v));
+            }
+        }
+        const float rec[6] = {p.x, p.y, p.z, q.x, q.y, q.z};
+        // the record is little-endian floats then bytes; both build hosts are little-endian
+        ok = std::fwrite(rec, sizeof(float), 6, f) == 6 && std::fwrite(rgb, 1, 3, f) == 3;
+    }
+    ok = (std::fclose(f) == 0) && ok;
+    if (!ok) return fail(h, KF_ERR_IO, std::string("short write to ") + path);
+    if (n_points) *n_points = (int)count;
+    return KF_OK;
+}
+
+namespace {
+
+// checkpoint file: this header, then the volume in the device layout (FP32: value plane
+// then weight plane; FP16: the half2 plane), then the predicted points and normals
+struct CheckpointHeader {
+    char magic[8];
+    uint32_t version;
+    int32_t height, width, dims[3], start[3], storage;
+    float voxel_size, truncated_distance, sdf_minimum, sdf_maximum;
+    float K[9];
+    float T[16];
+    double Td[16];
+    uint64_t volume_bytes, prediction_bytes;
+};
+constexpr char kCheckpointMagic[8] = {'K', 'F', 'G', 'B', '3', '0', '0', '\0'};
+
+void fill_header(const kf_handle* h, CheckpointHeader& c)
+{
+    std::memset(&c, 0, sizeof(c));
+    std::memcpy(c.magic, kCheckpointMagic, sizeof(c.magic));
+    c.version = 1;
+    c.height = h->cfg.height;
+    c.width = h->cfg.width;
+    for (int k = 0; k < 3; ++k) {
+        c.dims[k] = h->cfg.dims[k];
+        c.start[k] = h->cfg.grid_start[k];
+    }
+    c.storage = h->cfg.tsdf_storage;
+    c.voxel_size = h->cfg.voxel_size;
+    c.truncated_distance = h->cfg.truncated_distance;
+    c.sdf_minimum = h->cfg.sdf_minimum;
+    c.sdf_maximum = h->cfg.sdf_maximum;
+    for (int k = 0; k < 9; ++k) c.K[k] = h->cam.K[k];
+    c.volume_bytes = h->d_vol16 ? sizeof(__half2) * h->nvox : 2 * sizeof(float) * h->nvox;
+    c.prediction_bytes = 2 * sizeof(float4) * (size_t)h->cam.H * h->cam.W;
+}
+
+// streams count bytes between a device buffer and a file through a pinned staging buffer
+bool stream_file(FILE* f, void* dev, size_t count, bool to_file, cudaStream_t s)
+{
+    constexpr size_t kChunk = 64u << 20;
+    void* stage = nullptr;
+    if (cudaMallocHost(&stage, kChunk) != cudaSuccess) return false;
+    bool ok = true;
+    for (size_t off = 0; off < count && ok; off += kChunk) {
+        const size_t n = count - off < kChunk ? count - off : kChunk;
+        char* d = static_cast<char*>(dev) + off;
+        if (to_file) {
+            ok = cudaMemcpyAsync(stage, d, n, cudaMemcpyDeviceToHost, s) == cudaSuccess &&
+                 cudaStreamSynchronize(s) == cudaSuccess && std::fwrite(stage, 1, n, f) == n;
+        } else {
+            ok = std::fread(stage, 1, n, f) == n &&
+                 cudaMemcpyAsync(d, stage, n, cudaMemcpyHostToDevice, s) == cudaSuccess &&
+                 cudaStreamSynchronize(s) == cudaSuccess;
+        }
+    }
+    cudaFreeHost(stage);
+    return ok;
+}
+
+}  // namespace
+
+kf_status kf_save_checkpoint(kf_handle* h, const char* path)
+{
+    KF_HANDLE(h);
+    if (!path) return fail(h, KF_ERR_INVALID_ARGUMENT, "null path");
+    KF_CUDA(h, cudaStreamSynchronize(h->stream));
+    KF_CUDA(h, cudaMemcpy(h->h_state, h->d_state, sizeof(State), cudaMemcpyDeviceToHost));
+    CheckpointHeader c;
+    fill_header(h, c);
+    std::memcpy(c.T, h->h_state->T, sizeof(c.T));
+    std::memcpy(c.Td, h->h_state->Td, sizeof(c.Td));
+    FILE* f = std::fopen(path, "wb");
+    if (!f) return fail(h, KF_ERR_IO, std::string("cannot open ") + path);
+    bool ok = std::fwrite(&c, sizeof(c), 1, f) == 1;
+    const size_t plane = sizeof(float) * h->nvox, img = sizeof(float4) * (size_t)h->cam.H * h->cam.W;
+    if (h->d_vol16) {
+        ok = ok && stream_file(f, h->d_vol16, sizeof(__half2) * h->nvox, true, h->stream);
+    } else {
+        ok = ok && stream_file(f, h->d_tsdf, plane, true, h->stream);
+        ok = ok && stream_file(f, h->d_weight, plane, true, h->stream);
+    }
+    ok = ok && stream_file(f, h->d_pv, img, true, h->stream) && stream_file(f, h->d_pn, img, true, h->stream);
+    ok = (std::fclose(f) == 0) && ok;
+    if (!ok) return fail(h, KF_ERR_IO, std::string("writing checkpoint ") + path + " failed");
+    return KF_OK;
+}
+
+kf_status kf_load_checkpoint(kf_handle* h, const char* path)
+{
+    KF_HANDLE(h);
+    if (!path) return fail(h, KF_ERR_INVALID_ARGUMENT, "null path");
+    FILE* f = std::fopen(path, "rb");
+    if (!f) return fail(h, KF_ERR_IO, std::string("cannot open ") + path);
+    CheckpointHeader c, want;
+    fill_header(h, want);
+    if (std::fread(&c, sizeof(c), 1, f) != 1 || std::memcmp(c.magic, kCheckpointMagic, sizeof(c.magic)) != 0 ||
+        c.version != 1) {
+        std::fclose(f);
+        return fail(h, KF_ERR_IO, std::string(path) + " is not a kinfu_gb300 checkpoint");
+    }
+    const bool same = c.height == want.height && c.width == want.width && c.storage == want.storage &&
+                      std::memcmp(c.dims, want.dims, sizeof(c.dims)) == 0 &&
+                      std::memcmp(c.start, want.start, sizeof(c.start)) == 0 && c.voxel_size == want.voxel_size &&
+                      c.truncated_distance == want.truncated_distance && c.sdf_minimum == want.sdf_minimum &&
+                      c.sdf_maximum == want.sdf_maximum && c.volume_bytes == want.volume_bytes &&
+                      c.prediction_bytes == want.prediction_bytes;
+    if (!same) {
+        std::fclose(f);
+        return fail(h, KF_ERR_INVALID_ARGUMENT, "checkpoint was saved with another image size, grid or storage");
+    }
+    for (int k = 0; k < 16; ++k)
+        if (!std::isfinite(c.T[k]) || !std::isfinite(c.Td[k])) {
+            std::fclose(f);
+            return fail(h, KF_ERR_IO, "checkpoint pose has a non-finite entry");
+        }
+    KF_CUDA(h, cudaStreamSynchronize(h->stream));
+    const size_t plane = sizeof(float) * h->nvox, img = sizeof(float4) * (size_t)h->cam.H * h->cam.W;
+    bool ok;
+    if (h->d_vol16) {
+        ok = stream_file(f, h->d_vol16, sizeof(__half2) * h->nvox, false, h->stream);
+    } else {
+        ok = stream_file(f, h->d_tsdf, plane, false, h->stream) && stream_file(f, h->d_weight, plane, false, h->stream);
+    }
+    ok = ok && stream_file(f, h->d_pv, img, false, h->stream) && stream_file(f, h->d_pn, img, false, h->stream);
+    std::fclose(f);
+    if (!ok) return fail(h, KF_ERR_IO, std::string("reading checkpoint ") + path + " failed");
+    kf_status s = kf_set_intrinsics(h, c.K[0], c.K[4], c.K[2], c.K[5]);
+    if (s != KF_OK) return s;
+    std::memcpy(h->h_state->T, c.T, sizeof(c.T));
+    std::memcpy(h->h_state->Td, c.Td, sizeof(c.Td));
+    KF_CUDA(h, cudaMemcpy(field_ptr<float>(h->d_state, offsetof(State, T)), c.T, sizeof(c.T), cudaMemcpyHostToDevice));
+    KF_CUDA(h, cudaMemcpy(field_ptr<double>(h->d_state, offsetof(State, Td)), c.Td, sizeof(c.Td),
+                          cudaMemcpyHostToDevice));
     return KF_OK;
 }
 

@@ -283,3 +283,36 @@ void launch_zfast_to_half2(const float* tsdf, const float* weight, __half2* dst,
 }
 
 }  // namespace kf
+
+namespace kf {
+namespace {
+
+// The predicted points with surface_prediction_z != 0 (threeD_viewer.cpp:26), packed:
+// (x, y, z, pixel index as int bits) and (nx, ny, nz, 0).  One atomic per warp.
+__global__ void __launch_bounds__(256) compact_cloud_kernel(const float4* __restrict__ pv,
+                                                            const float4* __restrict__ pn, int n,
+                                                            float4* __restrict__ out, unsigned* count)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    const float4 p = i < n ? pv[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const bool keep = i < n && p.z != 0.f;
+    const unsigned mask = __ballot_sync(0xffffffffu, keep);
+    unsigned base = 0;
+    if (lane == 0 && mask) base = atomicAdd(count, (unsigned)__popc(mask));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (!keep) return;
+    const unsigned k = base + __popc(mask & ((1u << lane) - 1u));
+    const float4 q = pn[i];
+    out[2 * k] = make_float4(p.x, p.y, p.z, __int_as_float(i));
+    out[2 * k + 1] = make_float4(q.x, q.y, q.z, 0.f);
+}
+
+}  // namespace
+
+void launch_compact_cloud(const float4* pv, const float4* pn, int n, float4* out, unsigned* count, cudaStream_t s)
+{
+    compact_cloud_kernel<<<(n + 255) / 256, 256, 0, s>>>(pv, pn, n, out, count);
+}
+
+}  // namespace kf

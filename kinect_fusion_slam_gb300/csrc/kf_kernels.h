@@ -63,6 +63,9 @@ int raycast_blocks();
 
 // st->c_flip from the device's own double acos (single thread, once per handle)
 void launch_calibrate(State* st, cudaStream_t s);
+// packs the predicted points with z != 0 into out (2 float4 per point, unordered) and
+// counts them into *count (zero on entry)
+void launch_compact_cloud(const float4* pv, const float4* pn, int n, float4* out, unsigned* count, cudaStream_t s);
 // identity pose, zeroed ICP bookkeeping and error flag (c_flip kept)
 void launch_state_reset(State* st, cudaStream_t s);
 

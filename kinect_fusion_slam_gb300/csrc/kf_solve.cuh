@@ -150,7 +150,7 @@ __device__ __forceinline__ bool rsqrt_round_f32(float h, float l, float E, float
 // decide it.  Out of line, so the compiler keeps them behind a branch instead of
 // issuing their FP64 instructions under a predicate on every call.
 // pivot of row j: sets *fail or L[j][j]
-__device__ __noinline__ void pivot_f64(float* L, int j, int* fail)
+static __device__ __noinline__ void pivot_f64(float* L, int j, int* fail)
 {
     double sd = L[j * 6 + j];
     for (int k = 0; k < j; ++k) {
@@ -164,7 +164,7 @@ __device__ __noinline__ void pivot_f64(float* L, int j, int* fail)
 }
 
 // off-diagonal entry (i, j) of the factor from A[i][j]
-__device__ __noinline__ float offdiag_f64(const float* L, int i, int j)
+static __device__ __noinline__ float offdiag_f64(const float* L, int i, int j)
 {
     double sd = L[i * 6 + j];
     for (int k = 0; k < j; ++k) sd -= L[i * 6 + k] * L[j * 6 + k];
@@ -172,7 +172,7 @@ __device__ __noinline__ float offdiag_f64(const float* L, int i, int j)
 }
 
 // forward (dir 0) or backward (dir 1) substitution entry i
-__device__ __noinline__ float subst_f64(const float* L, const float* x, int i, int dir)
+static __device__ __noinline__ float subst_f64(const float* L, const float* x, int i, int dir)
 {
     double sd = x[i];
     if (dir == 0)
@@ -183,7 +183,7 @@ __device__ __noinline__ float subst_f64(const float* L, const float* x, int i, i
 }
 
 // entry (r, c) of mat4(a, b)
-__device__ __noinline__ float mat4_entry_f64(const float* a, const float* b, int r, int c)
+static __device__ __noinline__ float mat4_entry_f64(const float* a, const float* b, int r, int c)
 {
     double s = (double)a[r * 4 + 0] * b[c];
     s += (double)a[r * 4 + 1] * b[4 + c];
