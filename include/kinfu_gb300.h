@@ -214,6 +214,46 @@ kf_status kf_export_ply(kf_handle* h, const char* path, const uint8_t* colour_bg
 kf_status kf_save_checkpoint(kf_handle* h, const char* path);
 kf_status kf_load_checkpoint(kf_handle* h, const char* path);
 
+/* ---- differentiation form: trilinear rendering of a TSDF and its adjoint ----------
+ * No counterpart in the reference (its ray cast, kf_ray_casting, is not
+ * differentiable).  The TSDF is a device float volume in this library's layout
+ * (x-fastest, value at voxel centre (index + start + 0.5) * voxel_size, NaN =
+ * unobserved), e.g. the handle's FP32 volume.  Per pixel (1-based u, v) the ray
+ * o + t R K^-1 [u, v, 1] (t = camera-z depth, mm) is marched from t_near to t_far in
+ * steps of `step`, the TSDF sampled trilinearly; the first pair of valid samples with
+ * f_a > 0 >= f_b gives depth t* = t_a + step f_a / (f_a - f_b) and the normal
+ * grad f / |grad f| at the crossing (world frame).  Pixels without one render 0. */
+typedef struct kf_render_desc {
+    int height, width;
+    float fx, fy, cx, cy; /* the reference's convention: 1-based principal point */
+    int dims[3];
+    int grid_start[3];
+    float voxel_size;
+    float t_near, t_far, step; /* mm, camera z */
+} kf_render_desc;
+/* depth: device H*W floats or NULL; normal: device H*W*3 floats or NULL; T: host 4x4
+ * row-major camera-to-world pose.  Asynchronous on stream. */
+kf_status kf_render_trilinear(const kf_render_desc* d, const float* tsdf, const float T[16], float* depth,
+                              float* normal, void* stream);
+/* The adjoint of kf_render_trilinear at (tsdf, T): given dL/d depth (H*W) and dL/d normal
+ * (H*W*3) on the device (either may be NULL), ADDS dL/d tsdf into grad_tsdf (device,
+ * volume-sized, or NULL) and dL/d xi into grad_pose (device, 6 floats, or NULL), where
+ * the pose is perturbed on the left, T(xi) = exp(xi^) T, xi = (omega, tau) in world
+ * coordinates.  Recomputes each ray; voxel gradients are added with atomics, so their
+ * low bits depend on the order of arrival.  Asynchronous on stream. */
+kf_status kf_render_trilinear_backward(const kf_render_desc* d, const float* tsdf, const float T[16],
+                                       const float* grad_depth, const float* grad_normal, float* grad_tsdf,
+                                       float* grad_pose, void* stream);
+/* Gauss-Newton sums of the depth residual r = rendered - measured over the pixels where
+ * both are nonzero and |r| <= max_residual (mm; <= 0: no gate -- the gate drops the
+ * occlusion edges, as ICP's 20 mm distance test does), with J = d rendered / d xi:
+ * sums[0..20] = J^T J (upper triangle row by row), sums[21..26] = J^T r, sums[27] =
+ * pixel count, sums[28] = sum r^2 (host, double).  measured_depth: device H*W floats
+ * (mm).  Synchronous. */
+kf_status kf_render_depth_normal_equations(const kf_render_desc* d, const float* tsdf, const float T[16],
+                                           const float* measured_depth, float max_residual, double sums[29],
+                                           void* stream);
+
 /* ---- timing --------------------------------------------------------------------- */
 /* per-stage device time of the latest kf_incoming_frame (CUDA events, ms):
  * [0] depth+vertex, [1] ICP, [2] integration, [3] ray cast, [4] whole frame.

@@ -70,6 +70,14 @@ class Config(C.Structure):
     ]
 
 
+class RenderDesc(C.Structure):
+    """kf_render_desc (include/kinfu_gb300.h): the differentiation form's camera and grid."""
+
+    _fields_ = [("height", C.c_int), ("width", C.c_int), ("fx", C.c_float), ("fy", C.c_float), ("cx", C.c_float),
+                ("cy", C.c_float), ("dims", C.c_int * 3), ("grid_start", C.c_int * 3), ("voxel_size", C.c_float),
+                ("t_near", C.c_float), ("t_far", C.c_float), ("step", C.c_float)]
+
+
 _f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
 _u16p = np.ctypeslib.ndpointer(np.uint16, flags="C_CONTIGUOUS")
 _vp = C.c_void_p
@@ -116,6 +124,11 @@ SIGNATURES = {
     "kf_export_ply": (C.c_int, [_H, C.c_char_p, C.c_void_p, C.POINTER(C.c_int)]),
     "kf_save_checkpoint": (C.c_int, [_H, C.c_char_p]),
     "kf_load_checkpoint": (C.c_int, [_H, C.c_char_p]),
+    "kf_render_trilinear": (C.c_int, [C.POINTER(RenderDesc), C.c_void_p, _f32p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "kf_render_trilinear_backward": (C.c_int, [C.POINTER(RenderDesc), C.c_void_p, _f32p, C.c_void_p, C.c_void_p,
+                                               C.c_void_p, C.c_void_p, C.c_void_p]),
+    "kf_render_depth_normal_equations": (C.c_int, [C.POINTER(RenderDesc), C.c_void_p, _f32p, C.c_void_p, C.c_float,
+                                                   C.POINTER(C.c_double), C.c_void_p]),
     "kf_selftest_solve": (C.c_int, [C.c_ulonglong, C.c_int, C.c_int, C.POINTER(C.c_ulonglong)]),
     "kf_icp_associate_noalloc": (C.c_int, [C.c_int, C.c_int, _f32p, _f32p, _f32p, _vp, _vp, _vp, _vp, C.c_float,
                                            C.c_float, _vp, _vp, _vp]),
