@@ -190,7 +190,7 @@ class Handle:
     def icp_stats(self, n: int | None = None, poses: bool = False):
         """Per-iteration correspondences and Cholesky success of the latest ICP (and the
         pose after each iteration when poses=True)."""
-        n = n or int(self.config.icp_iterations[0])
+        n = n or int(sum(self.config.icp_iterations[:max(1, int(self.config.icp_levels))]))
         nc = np.zeros(n, np.int32)
         ok = np.zeros(n, np.int32)
         Ts = np.zeros((n, 4, 4), np.float32) if poses else None

@@ -18,6 +18,8 @@
 
 using namespace kf;
 
+constexpr int kMaxLevels = 3;
+
 struct kf_handle {
     kf_config cfg{};
     Grid grid{};
@@ -45,6 +47,10 @@ struct kf_handle {
     unsigned* d_tiles = nullptr;  // ray-cast tile counter
     float* d_mats = nullptr;  // F, T (debug association input) + sums output
     float* d_spatial = nullptr;
+    // ICP pyramid: level 0 aliases the buffers above; levels 1.. are half size each
+    Camera lcam[kMaxLevels]{};
+    float* d_depth_l[kMaxLevels] = {};
+    float4 *d_vmap_l[kMaxLevels] = {}, *d_nmap_l[kMaxLevels] = {}, *d_pv_l[kMaxLevels] = {}, *d_pn_l[kMaxLevels] = {};
 
     uint16_t* h_raw = nullptr;  // pinned staging for pageable host input
     State* h_state = nullptr;   // pinned readback
@@ -112,13 +118,28 @@ bool validate(const kf_config* c, std::string& why)
         why = "voxel_size and truncated_distance must be positive";
         return false;
     }
-    if (c->icp_levels != 1) {
-        why = "only single-level ICP is implemented (icp_levels must be 1)";
+    if (c->icp_levels < 1 || c->icp_levels > kMaxLevels) {
+        why = "icp_levels must be 1 (the reference), 2 or 3";
         return false;
     }
-    if (c->icp_iterations[0] < 0 || c->icp_iterations[0] > kMaxIcpIters) {
-        why = "icp_iterations out of range [0, 64]";
+    int total = 0;
+    for (int l = 0; l < c->icp_levels; ++l) {
+        if (c->icp_iterations[l] < 0 || c->icp_iterations[l] > kMaxIcpIters) {
+            why = "icp_iterations out of range [0, 64]";
+            return false;
+        }
+        total += c->icp_iterations[l];
+    }
+    if (total > kMaxIcpIters) {
+        why = "more than 64 ICP iterations per frame";
         return false;
+    }
+    if (c->icp_levels > 1) {
+        const int f = 1 << (c->icp_levels - 1);
+        if (c->height % f || c->width % f || c->height / f < 8 || c->width / f < 8) {
+            why = "the pyramid needs height and width divisible by 2^(icp_levels-1), coarsest level >= 8x8";
+            return false;
+        }
     }
     if (c->icp_reduction != KF_REDUCE_REFERENCE_ORDER && c->icp_reduction != KF_REDUCE_TREE) {
         why = "unknown icp_reduction";
@@ -179,11 +200,26 @@ void enq_bilateral(kf_handle* h)
                     h->stream);
 }
 
+// ICP of one frame.  With a pyramid (not in the reference, which tracks at full
+// resolution only), the coarser levels' depth, vertex/normal maps and previous-frame
+// predictions are derived first, then the iterations run coarsest level first; the pose
+// carries over between levels.
 void enq_icp(kf_handle* h)
 {
-    for (int it = 0; it < h->cfg.icp_iterations[0]; ++it)
-        launch_icp_iteration(h->d_vmap, h->d_nmap, h->d_pv, h->d_pn, h->cam, h->icp, h->d_state, h->d_partials,
-                             h->d_groups, h->stream);
+    const int L = h->cfg.icp_levels;
+    for (int l = 1; l < L; ++l) {
+        const Camera& f = h->lcam[l - 1];
+        const Camera& c = h->lcam[l];
+        launch_pyramid_depth(h->d_depth_l[l - 1], f.W, h->d_depth_l[l], c.H, c.W, 3.0f * h->cfg.sigma_r, h->stream);
+        launch_vertex(nullptr, h->d_depth_l[l], h->d_vmap_l[l], h->d_nmap_l[l], c, h->cfg.min_depth, h->cfg.max_depth,
+                      h->d_state, false, true, h->stream);
+        launch_pyramid_prediction(h->d_pv_l[l - 1], h->d_pn_l[l - 1], f.W, h->d_pv_l[l], h->d_pn_l[l], c.H, c.W,
+                                  h->stream);
+    }
+    for (int l = L - 1; l >= 0; --l)
+        for (int it = 0; it < h->cfg.icp_iterations[l]; ++it)
+            launch_icp_iteration(h->d_vmap_l[l], h->d_nmap_l[l], h->d_pv_l[l], h->d_pn_l[l], h->lcam[l], h->icp,
+                                 h->d_state, h->d_partials, h->d_groups, h->stream);
 }
 
 void enq_integrate(kf_handle* h, bool first)
@@ -292,6 +328,19 @@ void set_camera(kf_handle* h, float fx, float fy, float cx, float cy)
     float K[9] = {fx, 0.0f, cx, 0.0f, fy, cy, 0.0f, 0.0f, 1.0f};
     std::memcpy(h->cam.K, K, sizeof(K));
     inv3(h->cam.K, h->cam.Ki);
+    h->lcam[0] = h->cam;
+    // level l halves the image l times: focal lengths / 2^l, and the 1-based principal
+    // point maps as (c - 1/2) / 2^l + 1/2 (pixel centres of the 2x2 blocks)
+    for (int l = 1; l < kMaxLevels; ++l) {
+        const float s = 1.0f / (float)(1 << l);
+        Camera& c = h->lcam[l];
+        c.H = h->cam.H >> l;
+        c.W = h->cam.W >> l;
+        const float Kl[9] = {fx * s, 0.0f, (cx - 0.5f) * s + 0.5f, 0.0f, fy * s, (cy - 0.5f) * s + 0.5f,
+                             0.0f, 0.0f, 1.0f};
+        std::memcpy(c.K, Kl, sizeof(Kl));
+        inv3(c.K, c.Ki);
+    }
 }
 
 template <class T>
@@ -333,6 +382,19 @@ kf_status allocate(kf_handle* h)
     KF_CUDA(h, cudaMemset(h->d_tiles, 0, 2 * sizeof(unsigned)));
     KF_TRY(dalloc(h, &h->d_mats, 64));
     KF_TRY(dalloc(h, &h->d_spatial, 15 * 15));
+    h->d_depth_l[0] = h->d_depth;
+    h->d_vmap_l[0] = h->d_vmap;
+    h->d_nmap_l[0] = h->d_nmap;
+    h->d_pv_l[0] = h->d_pv;
+    h->d_pn_l[0] = h->d_pn;
+    for (int l = 1; l < h->cfg.icp_levels; ++l) {
+        const size_t n = HW >> (2 * l);
+        KF_TRY(dalloc(h, &h->d_depth_l[l], n));
+        KF_TRY(dalloc(h, &h->d_vmap_l[l], n));
+        KF_TRY(dalloc(h, &h->d_nmap_l[l], n));
+        KF_TRY(dalloc(h, &h->d_pv_l[l], n));
+        KF_TRY(dalloc(h, &h->d_pn_l[l], n));
+    }
     if (h->cfg.tsdf_storage == KF_TSDF_F16) {
         KF_TRY(dalloc(h, &h->d_vol16, h->nvox));
     } else {
@@ -390,6 +452,11 @@ void free_all(kf_handle* h)
                    h->d_spatial};
     for (void* p : dev)
         if (p) cudaFree(p);
+    for (int l = 1; l < kMaxLevels; ++l) {
+        void* lv[] = {h->d_depth_l[l], h->d_vmap_l[l], h->d_nmap_l[l], h->d_pv_l[l], h->d_pn_l[l]};
+        for (void* p : lv)
+            if (p) cudaFree(p);
+    }
     if (h->h_raw) cudaFreeHost(h->h_raw);
     if (h->h_state) cudaFreeHost(h->h_state);
     for (auto& e : h->ev)
@@ -1129,7 +1196,9 @@ kf_status kf_kernels_per_frame(kf_handle* h, int* n)
     // reduction one pass each), integration prep, integration, ray cast
     const int per_iteration =
         (h->cfg.icp_reduction == KF_REDUCE_REFERENCE_ORDER && h->cfg.solve_mode != KF_SOLVE_PRECISE) ? 2 : 1;
-    *n = 1 + (h->cfg.bilateral ? 1 : 0) + per_iteration * h->cfg.icp_iterations[0] + 3;
+    int iterations = 0;
+    for (int l = 0; l < h->cfg.icp_levels; ++l) iterations += h->cfg.icp_iterations[l];
+    *n = 1 + (h->cfg.bilateral ? 1 : 0) + 3 * (h->cfg.icp_levels - 1) + per_iteration * iterations + 3;
     return KF_OK;
 }
 

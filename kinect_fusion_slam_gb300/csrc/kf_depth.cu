@@ -316,3 +316,59 @@ void launch_compact_cloud(const float4* pv, const float4* pn, int n, float4* out
 }
 
 }  // namespace kf
+
+namespace kf {
+namespace {
+
+// One level of the depth pyramid: coarse (i, j) averages the nonzero depths of the fine
+// 2x2 block (scan order: (2i,2j), (2i,2j+1), (2i+1,2j), (2i+1,2j+1)) that lie within
+// `band` of the block's first nonzero depth -- block averaging with a depth-similarity
+// test, so a block straddling an occlusion edge keeps the nearer surface instead of
+// inventing a depth between the two.  Zero where the block has no depth.
+__global__ void __launch_bounds__(256) pyramid_depth_kernel(const float* __restrict__ fine, int Wf,
+                                                            float* __restrict__ coarse, int Hc, int Wc, float band)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= Hc * Wc) return;
+    const int r = i / Wc, c = i % Wc;
+    const float d[4] = {fine[(2 * r) * Wf + 2 * c], fine[(2 * r) * Wf + 2 * c + 1], fine[(2 * r + 1) * Wf + 2 * c],
+                        fine[(2 * r + 1) * Wf + 2 * c + 1]};
+    float ref = 0.f;
+    for (int k = 0; k < 4 && ref == 0.f; ++k) ref = d[k];
+    float sum = 0.f;
+    int n = 0;
+    for (int k = 0; k < 4; ++k)
+        if (d[k] != 0.f && fabsf(d[k] - ref) <= band) {
+            sum = sum + d[k];
+            ++n;
+        }
+    coarse[i] = n ? sum / (float)n : 0.f;
+}
+
+// the previous frame's prediction at a coarser level: the fine pixel (2i, 2j)
+__global__ void __launch_bounds__(256) pyramid_prediction_kernel(const float4* __restrict__ pv_f,
+                                                                 const float4* __restrict__ pn_f, int Wf,
+                                                                 float4* __restrict__ pv_c, float4* __restrict__ pn_c,
+                                                                 int Hc, int Wc)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= Hc * Wc) return;
+    const int j = (2 * (i / Wc)) * Wf + 2 * (i % Wc);
+    pv_c[i] = pv_f[j];
+    pn_c[i] = pn_f[j];
+}
+
+}  // namespace
+
+void launch_pyramid_depth(const float* fine, int Wf, float* coarse, int Hc, int Wc, float band, cudaStream_t s)
+{
+    pyramid_depth_kernel<<<(Hc * Wc + 255) / 256, 256, 0, s>>>(fine, Wf, coarse, Hc, Wc, band);
+}
+
+void launch_pyramid_prediction(const float4* pv_f, const float4* pn_f, int Wf, float4* pv_c, float4* pn_c, int Hc,
+                               int Wc, cudaStream_t s)
+{
+    pyramid_prediction_kernel<<<(Hc * Wc + 255) / 256, 256, 0, s>>>(pv_f, pn_f, Wf, pv_c, pn_c, Hc, Wc);
+}
+
+}  // namespace kf

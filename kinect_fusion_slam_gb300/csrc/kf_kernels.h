@@ -63,6 +63,11 @@ int raycast_blocks();
 
 // st->c_flip from the device's own double acos (single thread, once per handle)
 void launch_calibrate(State* st, cudaStream_t s);
+// ICP pyramid (not in the reference): 2x2 block-averaged depth with a similarity band,
+// and the fine level's prediction subsampled at (2i, 2j)
+void launch_pyramid_depth(const float* fine, int Wf, float* coarse, int Hc, int Wc, float band, cudaStream_t s);
+void launch_pyramid_prediction(const float4* pv_f, const float4* pn_f, int Wf, float4* pv_c, float4* pn_c, int Hc,
+                               int Wc, cudaStream_t s);
 // packs the predicted points with z != 0 into out (2 float4 per point, unordered) and
 // counts them into *count (zero on entry)
 void launch_compact_cloud(const float4* pv, const float4* pn, int n, float4* out, unsigned* count, cudaStream_t s);

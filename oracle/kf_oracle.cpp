@@ -481,18 +481,21 @@ void kfo_icp_terms(int H, int W, const float* K, const float* F, const float* T,
     }
 }
 
-void kfo_estimate_pose(int H, int W, const float* K, float* T, const float* cur6, const uint8_t* mask,
-                       const float* pred6, int iters, float* sums_log, float* pose_log, int32_t* ncorr_log,
-                       int32_t* chol_ok_log)
+namespace {
+
+/* the ICP iterations of sensor_pose_estimation.cu:339-429 from a given T_prev^-1 (the
+ * frame start's, :256), updating R in place */
+void pose_iterations(int H, int W, const float* K, const float* Tprev_inv, float* R, const float* cur6,
+                     const uint8_t* mask, const float* pred6, int iters, int log0, float* sums_log, float* pose_log,
+                     int32_t* ncorr_log, int32_t* chol_ok_log)
 {
-    float Tprev_inv[16], R[16], F[16];
-    ocv_inv4(T, Tprev_inv);
-    std::memcpy(R, T, sizeof(R));
+    float F[16];
     for (int it = 0; it < iters; ++it) {
         ocv_matmul4(Tprev_inv, R, F);
         float s42[42];
         const int nc = kfo_icp_associate(H, W, K, F, R, cur6, mask, pred6, nullptr, s42);
-        if (sums_log) std::memcpy(sums_log + it * 42, s42, sizeof(s42));
+        const int q = log0 + it;
+        if (sums_log) std::memcpy(sums_log + q * 42, s42, sizeof(s42));
         float A[36], x[6];
         for (int k = 0; k < 36; ++k) A[k] = s42[6 + k];
         for (int k = 0; k < 6; ++k) x[k] = s42[k];
@@ -502,11 +505,56 @@ void kfo_estimate_pose(int H, int W, const float* K, float* T, const float* cur6
         const float inc[16] = {1.0f, x[2], -x[1], x[3], -x[2], 1.0f, x[0], x[4],
                                x[1], -x[0], 1.0f, x[5], 0.0f, 0.0f, 0.0f, 1.0f};
         ocv_matmul4(inc, R, R);
-        if (pose_log) std::memcpy(pose_log + it * 16, R, sizeof(R));
-        if (ncorr_log) ncorr_log[it] = nc;
-        if (chol_ok_log) chol_ok_log[it] = ok;
+        if (pose_log) std::memcpy(pose_log + q * 16, R, sizeof(float) * 16);
+        if (ncorr_log) ncorr_log[q] = nc;
+        if (chol_ok_log) chol_ok_log[q] = ok;
     }
+}
+
+}  // namespace
+
+void kfo_estimate_pose(int H, int W, const float* K, float* T, const float* cur6, const uint8_t* mask,
+                       const float* pred6, int iters, float* sums_log, float* pose_log, int32_t* ncorr_log,
+                       int32_t* chol_ok_log)
+{
+    float Tprev_inv[16], R[16];
+    ocv_inv4(T, Tprev_inv);
+    std::memcpy(R, T, sizeof(R));
+    pose_iterations(H, W, K, Tprev_inv, R, cur6, mask, pred6, iters, 0, sums_log, pose_log, ncorr_log, chol_ok_log);
     std::memcpy(T, R, sizeof(R));
+}
+
+/* ICP pyramid (not in the reference): coarse (i, j) averages the nonzero depths of the
+ * fine 2x2 block, scan order (2i,2j), (2i,2j+1), (2i+1,2j), (2i+1,2j+1), that lie within
+ * band of the block's first nonzero depth; 0 where the block has none */
+void kfo_pyramid_depth(int Hf, int Wf, const float* fine, float band, float* coarse)
+{
+    const int Hc = Hf / 2, Wc = Wf / 2;
+    for (int r = 0; r < Hc; ++r)
+        for (int c = 0; c < Wc; ++c) {
+            const float d[4] = {fine[(2 * r) * Wf + 2 * c], fine[(2 * r) * Wf + 2 * c + 1],
+                                fine[(2 * r + 1) * Wf + 2 * c], fine[(2 * r + 1) * Wf + 2 * c + 1]};
+            float ref = 0.f;
+            for (int k = 0; k < 4 && ref == 0.f; ++k) ref = d[k];
+            float sum = 0.f;
+            int n = 0;
+            for (int k = 0; k < 4; ++k)
+                if (d[k] != 0.f && std::fabs(d[k] - ref) <= band) {
+                    sum = sum + d[k];
+                    ++n;
+                }
+            coarse[r * Wc + c] = n ? sum / (float)n : 0.f;
+        }
+}
+
+/* the intrinsics of pyramid level l: focal lengths / 2^l, 1-based principal point
+ * (c - 1/2) / 2^l + 1/2 */
+void kfo_level_intrinsics(const float* K, int l, float* Kl)
+{
+    const float s = 1.0f / (float)(1 << l);
+    const float k[9] = {K[0] * s, 0.0f, (K[2] - 0.5f) * s + 0.5f, 0.0f, K[4] * s, (K[5] - 0.5f) * s + 0.5f,
+                        0.0f, 0.0f, 1.0f};
+    std::memcpy(Kl, k, sizeof(k));
 }
 
 /* bilateral_filtering.cu:3-47 */
@@ -545,6 +593,8 @@ struct kfo_pipeline {
     kfo_grid g;
     float K[9], Ki[9], T[16];
     int icp_iters;
+    int levels = 1, level_iters[3] = {10, 0, 0};
+    float band = 90.f;
     std::vector<float> tsdf, weight, depth, cur6, pred6;
     std::vector<uint8_t> mask;
     std::vector<int32_t> hit;
@@ -587,6 +637,13 @@ void kfo_initial(kfo_pipeline* p, const uint16_t* raw)
     kfo_raycast(&p->g, H, W, p->depth.data(), p->Ki, p->T, p->tsdf.data(), p->pred6.data(), p->hit.data());
 }
 
+void kfo_set_pyramid(kfo_pipeline* p, int levels, const int* iters, float band)
+{
+    p->levels = levels < 1 ? 1 : (levels > 3 ? 3 : levels);
+    for (int l = 0; l < 3; ++l) p->level_iters[l] = l < p->levels ? iters[l] : 0;
+    p->band = band;
+}
+
 void kfo_incoming(kfo_pipeline* p, const uint16_t* raw)
 {
     const int H = p->H, W = p->W;
@@ -595,8 +652,44 @@ void kfo_incoming(kfo_pipeline* p, const uint16_t* raw)
     float* c = p->cur6.data();
     kfo_vertex_normal(H, W, p->depth.data(), p->Ki, c, c + HW, c + 3 * HW, c + 4 * HW, c + 5 * HW, p->mask.data());
     std::memcpy(c + 2 * HW, p->depth.data(), sizeof(float) * HW);
-    kfo_estimate_pose(H, W, p->K, p->T, c, p->mask.data(), p->pred6.data(), p->icp_iters, nullptr, nullptr, nullptr,
-                      nullptr);
+    if (p->levels == 1) {
+        kfo_estimate_pose(H, W, p->K, p->T, c, p->mask.data(), p->pred6.data(), p->icp_iters, nullptr, nullptr,
+                          nullptr, nullptr);
+    } else {
+        /* per level: depth, K, vertex/normal map (cur6 layout) and the previous
+         * prediction subsampled at (2i, 2j) */
+        std::vector<float> depth[3], cur[3], pred[3];
+        std::vector<uint8_t> mask[3];
+        float Kl[3][9];
+        depth[0] = p->depth;
+        cur[0] = p->cur6;
+        pred[0] = p->pred6;
+        mask[0] = p->mask;
+        std::memcpy(Kl[0], p->K, sizeof(Kl[0]));
+        for (int l = 1; l < p->levels; ++l) {
+            const int Hf = H >> (l - 1), Wf = W >> (l - 1), Hc = H >> l, Wc = W >> l;
+            const long n = (long)Hc * Wc, nf = (long)Hf * Wf;
+            depth[l].assign(n, 0.f);
+            kfo_pyramid_depth(Hf, Wf, depth[l - 1].data(), p->band, depth[l].data());
+            kfo_level_intrinsics(p->K, l, Kl[l]);
+            float Kil[9];
+            ocv_inv3(Kl[l], Kil);
+            cur[l].assign(6 * n, 0.f);
+            mask[l].assign(n, 0);
+            float* q = cur[l].data();
+            kfo_vertex_normal(Hc, Wc, depth[l].data(), Kil, q, q + n, q + 3 * n, q + 4 * n, q + 5 * n, mask[l].data());
+            std::memcpy(q + 2 * n, depth[l].data(), sizeof(float) * n);
+            pred[l].assign(6 * n, 0.f);
+            for (int k = 0; k < 6; ++k)
+                for (long i = 0; i < n; ++i)
+                    pred[l][k * n + i] = pred[l - 1][k * nf + (2 * (i / Wc)) * Wf + 2 * (i % Wc)];
+        }
+        float Tprev_inv[16];
+        ocv_inv4(p->T, Tprev_inv);
+        for (int l = p->levels - 1; l >= 0; --l)
+            pose_iterations(H >> l, W >> l, Kl[l], Tprev_inv, p->T, cur[l].data(), mask[l].data(), pred[l].data(),
+                            p->level_iters[l], 0, nullptr, nullptr, nullptr, nullptr);
+    }
     float Ti[16];
     ocv_inv4(p->T, Ti);
     kfo_integrate(&p->g, H, W, p->depth.data(), p->K, p->Ki, p->T, Ti, p->tsdf.data(), p->weight.data(), 0);

@@ -90,6 +90,11 @@ void kfo_destroy(kfo_pipeline* p);
 void kfo_initial(kfo_pipeline* p, const uint16_t* raw);
 /* IncomingFrameProcessing (kinfu_pipeline.cpp:121-193), bilateral disabled as in the reference */
 void kfo_incoming(kfo_pipeline* p, const uint16_t* raw);
+/* ICP pyramid (not in the reference): levels 1..3, iterations per level finest first,
+ * depth-similarity band of the block averaging (mm) */
+void kfo_set_pyramid(kfo_pipeline* p, int levels, const int* iters, float band);
+void kfo_pyramid_depth(int Hf, int Wf, const float* fine, float band, float* coarse);
+void kfo_level_intrinsics(const float* K, int l, float* Kl);
 void kfo_get_pose(const kfo_pipeline* p, float* T);
 void kfo_set_pose(kfo_pipeline* p, const float* T);
 /* 6 planes HxW (x,y,z,nx,ny,nz), and the hit plane */

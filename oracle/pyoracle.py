@@ -150,6 +150,10 @@ class Oracle(_Common):
         self._fn("kfo_get_depth", None, [C.c_void_p, _f32p])
         self._fn("kfo_get_vertex_map", None, [C.c_void_p, C.c_void_p, C.c_void_p])
         self._fn("kfo_num_threads", C.c_int, [])
+        self._fn("kfo_set_pyramid", None, [C.c_void_p, C.c_int, np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS"),
+                                           C.c_float])
+        self._fn("kfo_pyramid_depth", None, [C.c_int, C.c_int, _f32p, C.c_float, _f32p])
+        self._fn("kfo_level_intrinsics", None, [_f32p, C.c_int, _f32p])
         self._fn("kfo_icp_terms", None, [C.c_int, C.c_int, _f32p, _f32p, _f32p, _f32p, _u8p, _f32p, _f32p])
         _f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
         self._fn("kfo64_create", C.c_void_p, [C.c_int, C.c_int, C.c_double, C.c_double, C.POINTER(Grid), _f64p,
@@ -202,6 +206,18 @@ class Oracle(_Common):
         self.lib.kfo_estimate_pose(H, W, _c32(K), T, _c32(cur6), np.ascontiguousarray(mask, np.uint8), _c32(pred6),
                                    iters, _nullable(sums), _nullable(poses), _nullable(ncorr), _nullable(ok))
         return T, {"sums": sums, "poses": poses.reshape(iters, 4, 4), "ncorr": ncorr, "chol_ok": ok}
+
+    def pyramid_depth(self, depth, band=90.0):
+        depth = _c32(depth)
+        H, W = depth.shape
+        out = np.zeros((H // 2, W // 2), np.float32)
+        self.lib.kfo_pyramid_depth(H, W, depth.ravel(), band, out.ravel())
+        return out
+
+    def level_intrinsics(self, K, level):
+        out = np.zeros(9, np.float32)
+        self.lib.kfo_level_intrinsics(_c32(K).ravel(), int(level), out)
+        return out.reshape(3, 3)
 
     def icp_terms(self, K, F, T, cur6, mask, pred6):
         """(H*W, 42) per-pixel ICP products: a*b (6) then a a^T (36); zero off correspondences."""
@@ -289,6 +305,12 @@ class OraclePipeline:
 
     def incoming(self, raw):
         self.o.lib.kfo_incoming(self.h, np.ascontiguousarray(raw, np.uint16).ravel())
+
+    def set_pyramid(self, levels, iterations, band=90.0):
+        """ICP pyramid: iterations per level, finest first."""
+        it = np.zeros(3, np.int32)
+        it[:len(iterations)] = iterations
+        self.o.lib.kfo_set_pyramid(self.h, int(levels), it, float(band))
 
     @property
     def pose(self):

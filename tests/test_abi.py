@@ -53,8 +53,8 @@ def test_reference_defaults():
 
 @pytest.mark.parametrize("field,value", [
     ("height", 0), ("width", 1), ("dims", (2, 360, 300)), ("dims", (5000, 360, 300)),
-    ("dims", (2048, 2048, 1024)), ("voxel_size", 0.0), ("truncated_distance", -1.0), ("icp_levels", 2),
-    ("icp_iterations", (65,)), ("tsdf_storage", 7), ("bilateral_radius", 8),
+    ("dims", (2048, 2048, 1024)), ("voxel_size", 0.0), ("truncated_distance", -1.0), ("icp_levels", 4),
+    ("icp_levels", 0), ("icp_iterations", (65,)), ("tsdf_storage", 7), ("bilateral_radius", 8),
 ])
 def test_invalid_config_rejected_without_device(field, value):
     lib = _lib.load()
@@ -62,6 +62,15 @@ def test_invalid_config_rejected_without_device(field, value):
     h = _lib._H()
     assert lib.kf_create(C.byref(cfg), C.byref(h)) == _lib.KF_ERR_INVALID_ARGUMENT
     assert not h.value
+
+
+def test_pyramid_config_limits():
+    lib = _lib.load()
+    h = _lib._H()
+    # 3 levels need the size divisible by 4; 60 iterations per level exceed 64 per frame
+    for kw in ({"icp_levels": 3, "height": 482}, {"icp_levels": 2, "icp_iterations": (40, 30)}):
+        cfg = kf.make_config(**kw)
+        assert lib.kf_create(C.byref(cfg), C.byref(h)) == _lib.KF_ERR_INVALID_ARGUMENT
 
 
 def test_null_arguments():
