@@ -254,6 +254,34 @@ kf_status kf_render_depth_normal_equations(const kf_render_desc* d, const float*
                                            const float* measured_depth, float max_residual, double sums[29],
                                            void* stream);
 
+/* ---- batching form: many scenes, one launch per stage, one graph per frame --------
+ * No counterpart in the reference.  A batch owns one kf_handle per scene; the scenes
+ * may differ in image size and grid, and share the TSDF storage, the ICP schedule
+ * (levels and iterations), the reference-order reduction and the float solve (no
+ * bilateral).  Each frame runs every stage as one launch over all scenes (the ray cast
+ * is persistent over all scenes' tiles), the whole frame captured as one CUDA graph.
+ * Each scene's results are bit-identical to running its handle alone. */
+typedef struct kf_batch kf_batch;
+kf_status kf_batch_create(const kf_config* configs, int n_scenes, kf_batch** out);
+kf_status kf_batch_destroy(kf_batch* b);
+/* the scene's handle (owned by the batch; do not destroy): intrinsics, pose, volume,
+ * prediction, statistics and checkpoints through the kf_* calls, on the batch's stream */
+kf_status kf_batch_scene(kf_batch* b, int scene, kf_handle** out);
+/* one frame of every scene: depth[i] = scene i's H_i*W_i uint16 depth in device memory
+ * (host array of n_scenes device pointers).  Asynchronous on the batch's stream. */
+kf_status kf_batch_initial_processing_device(kf_batch* b, const uint16_t* const* depth);
+kf_status kf_batch_incoming_frame_device(kf_batch* b, const uint16_t* const* depth);
+kf_status kf_batch_synchronize(kf_batch* b);
+/* kernels one kf_batch_incoming_frame_device launches (for all scenes together) */
+kf_status kf_batch_kernels_per_frame(kf_batch* b, int* n);
+/* Autotuner: times the candidate launch shapes of the idempotent batched stages on the
+ * batch's current data (run after a frame) and keeps the fastest: tuning[0] = ICP group
+ * pass warps per block (4, 8, 16), [1] = ray-cast tile shape (0: 8x4, 1: 16x2, 2: 4x8
+ * pixels per warp), [2] = ray-cast blocks per SM (1..4), [3] = integration z chunk
+ * (8, 16, 32; not timed: integration updates the volume).  Synchronous. */
+kf_status kf_batch_autotune(kf_batch* b, int tuning[4]);
+kf_status kf_batch_set_tuning(kf_batch* b, const int tuning[4]);
+
 /* ---- timing --------------------------------------------------------------------- */
 /* per-stage device time of the latest kf_incoming_frame (CUDA events, ms):
  * [0] depth+vertex, [1] ICP, [2] integration, [3] ray cast, [4] whole frame.

@@ -23,7 +23,7 @@ from . import _lib
 from ._lib import (KF_ICP_FAIL_IDENTITY, KF_ICP_FAIL_REFERENCE, KF_REDUCE_REFERENCE_ORDER, KF_REDUCE_TREE,
                    KF_SOLVE_PRECISE, KF_SOLVE_REFERENCE, KF_TSDF_F16, KF_TSDF_F32, Config, KinfuError)
 
-__all__ = ["KinfuPipeline", "Handle", "Config", "KinfuError", "make_config", "KF_TSDF_F32", "KF_TSDF_F16",
+__all__ = ["KinfuPipeline", "Handle", "Batch", "Config", "KinfuError", "make_config", "KF_TSDF_F32", "KF_TSDF_F16",
            "KF_ICP_FAIL_REFERENCE", "KF_ICP_FAIL_IDENTITY", "KF_SOLVE_REFERENCE", "KF_SOLVE_PRECISE",
            "KF_REDUCE_REFERENCE_ORDER", "KF_REDUCE_TREE"]
 
@@ -68,7 +68,22 @@ class Handle:
         if st != _lib.KF_OK:
             raise KinfuError(st, self.lib.kf_last_error(self.h).decode())
 
+    @classmethod
+    def _borrowed(cls, ptr, config: Config, owner) -> "Handle":
+        """A view of a handle owned elsewhere (a batch's scene); closing it does nothing."""
+        self = cls.__new__(cls)
+        self.lib = _lib.load()
+        self.config = config
+        self.h = ptr
+        self.H, self.W = config.height, config.width
+        self.dims = tuple(config.dims)
+        self._owner = owner
+        return self
+
     def close(self) -> None:
+        if getattr(self, "_owner", None) is not None:
+            self.h = None
+            return
         if getattr(self, "h", None):
             self.lib.kf_destroy(self.h)
             self.h = None
@@ -323,3 +338,68 @@ class KinfuPipeline:
 
     def close(self) -> None:
         self.handle.close()
+
+
+class Batch:
+    """The batching form (kf_batch_*): independent scenes of uneven image and grid
+    sizes, every stage one launch for all of them, each frame one CUDA graph."""
+
+    def __init__(self, configs):
+        self.lib = _lib.load()
+        self.configs = list(configs)
+        arr = (Config * len(self.configs))(*self.configs)
+        b = C.c_void_p()
+        st = self.lib.kf_batch_create(arr, len(self.configs), C.byref(b))
+        if st != _lib.KF_OK:
+            raise KinfuError(st, "kf_batch_create failed")
+        self.b = b
+        self.scenes = []
+        for i, cfg in enumerate(self.configs):
+            h = _lib._H()
+            self._check(self.lib.kf_batch_scene(self.b, i, C.byref(h)))
+            self.scenes.append(Handle._borrowed(h, cfg, self))
+
+    def _check(self, st: int) -> None:
+        if st != _lib.KF_OK:
+            raise KinfuError(st, "kf_batch call failed")
+
+    def close(self) -> None:
+        if getattr(self, "b", None):
+            for h in self.scenes:
+                h.h = None
+            self.lib.kf_batch_destroy(self.b)
+            self.b = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _ptrs(self, dev_ptrs):
+        if len(dev_ptrs) != len(self.scenes):
+            raise ValueError("one depth pointer per scene")
+        return (C.c_void_p * len(dev_ptrs))(*[C.c_void_p(int(p)) for p in dev_ptrs])
+
+    def initial_processing_device(self, dev_ptrs) -> None:
+        self._check(self.lib.kf_batch_initial_processing_device(self.b, self._ptrs(dev_ptrs)))
+
+    def incoming_frame_device(self, dev_ptrs) -> None:
+        self._check(self.lib.kf_batch_incoming_frame_device(self.b, self._ptrs(dev_ptrs)))
+
+    def synchronize(self) -> None:
+        self._check(self.lib.kf_batch_synchronize(self.b))
+
+    def kernels_per_frame(self) -> int:
+        n = C.c_int(0)
+        self._check(self.lib.kf_batch_kernels_per_frame(self.b, C.byref(n)))
+        return n.value
+
+    def autotune(self) -> tuple:
+        t = (C.c_int * 4)()
+        self._check(self.lib.kf_batch_autotune(self.b, t))
+        return tuple(t)
+
+    def set_tuning(self, tuning) -> None:
+        self._check(self.lib.kf_batch_set_tuning(self.b, (C.c_int * 4)(*tuning)))
+

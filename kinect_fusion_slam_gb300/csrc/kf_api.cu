@@ -15,53 +15,10 @@
 
 #include "kinfu_gb300.h"
 #include "kf_kernels.h"
+#include "kf_handle.h"
 
 using namespace kf;
 
-constexpr int kMaxLevels = 3;
-
-struct kf_handle {
-    kf_config cfg{};
-    Grid grid{};
-    Camera cam{};
-    IcpParams icp{};
-    int device = 0;
-    cudaStream_t stream = nullptr;      // stream all work goes to
-    cudaStream_t own_stream = nullptr;  // the handle's own stream
-    size_t nvox = 0;
-    long long skip_from = 0;  // first z-fastest voxel index the reference never integrates
-
-    uint16_t* d_raw = nullptr;
-    float* d_depth = nullptr;
-    float* d_depth_tmp = nullptr;  // bilateral output
-    float4 *d_vmap = nullptr, *d_nmap = nullptr, *d_pv = nullptr, *d_pn = nullptr;
-    int32_t* d_hit = nullptr;
-    int32_t* d_pair = nullptr;
-    float2* d_tab = nullptr;
-    float* d_tsdf = nullptr;
-    float* d_weight = nullptr;
-    __half2* d_vol16 = nullptr;
-    State* d_state = nullptr;
-    float* d_partials = nullptr;
-    int* d_groups = nullptr;  // ICP group flags / compacted group list
-    unsigned* d_tiles = nullptr;  // ray-cast tile counter
-    float* d_mats = nullptr;  // F, T (debug association input) + sums output
-    float* d_spatial = nullptr;
-    // ICP pyramid: level 0 aliases the buffers above; levels 1.. are half size each
-    Camera lcam[kMaxLevels]{};
-    float* d_depth_l[kMaxLevels] = {};
-    float4 *d_vmap_l[kMaxLevels] = {}, *d_nmap_l[kMaxLevels] = {}, *d_pv_l[kMaxLevels] = {}, *d_pn_l[kMaxLevels] = {};
-
-    uint16_t* h_raw = nullptr;  // pinned staging for pageable host input
-    State* h_state = nullptr;   // pinned readback
-
-    cudaGraphExec_t g_incoming = nullptr, g_initial = nullptr;
-    bool timing = false;
-    cudaEvent_t ev[5] = {};
-    float stage_ms[5] = {};
-    bool frame_timed = false;
-    std::string err;
-};
 
 namespace {
 

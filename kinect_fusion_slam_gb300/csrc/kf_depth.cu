@@ -30,12 +30,11 @@ __device__ __forceinline__ float ingest(uint16_t raw, float dmin, float dmax)
 
 // raw_vertices.cu:3-51.  One thread per pixel; the mask is kept in vmap.w.
 template <bool RAW>
-__global__ void __launch_bounds__(256) vertex_kernel(const uint16_t* __restrict__ raw, float* __restrict__ depth,
-                                                     float4* __restrict__ vmap, float4* __restrict__ nmap, Camera cam,
-                                                     float dmin, float dmax, State* st, int init_icp, int normals)
+__device__ __forceinline__ void vertex_body(int i, const uint16_t* __restrict__ raw, float* __restrict__ depth,
+                                            float4* __restrict__ vmap, float4* __restrict__ nmap, const Camera& cam,
+                                            float dmin, float dmax, State* st, int init_icp, int normals)
 {
     const int H = cam.H, W = cam.W;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (init_icp && i == 0) {
         // frame start of Estimate_Sensor_Pose (sensor_pose_estimation.cu:255-259, 343)
         inv4(st->T, st->Tprev_inv);
@@ -82,6 +81,30 @@ __global__ void __launch_bounds__(256) vertex_kernel(const uint16_t* __restrict_
     }
     vmap[i] = v;
     nmap[i] = n;
+}
+
+template <bool RAW>
+__global__ void __launch_bounds__(256) vertex_kernel(const uint16_t* __restrict__ raw, float* __restrict__ depth,
+                                                     float4* __restrict__ vmap, float4* __restrict__ nmap, Camera cam,
+                                                     float dmin, float dmax, State* st, int init_icp, int normals)
+{
+    vertex_body<RAW>(blockIdx.x * blockDim.x + threadIdx.x, raw, depth, vmap, nmap, cam, dmin, dmax, st, init_icp,
+                     normals);
+}
+
+// every scene of a batch: level 0 from the raw depth (with the ICP set-up), or level l
+// from that level's depth
+__global__ void __launch_bounds__(256) vertex_batch_kernel(const SceneDev* __restrict__ scenes, int level,
+                                                           int init_icp)
+{
+    const SceneDev& d = scenes[blockIdx.y];
+    const Camera& cam = d.cam[level];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= cam.H * cam.W && !(init_icp && i == 0)) return;
+    if (level == 0)
+        vertex_body<true>(i, d.raw, d.depth[0], d.vmap[0], d.nmap[0], cam, d.dmin, d.dmax, d.st, init_icp, 1);
+    else
+        vertex_body<false>(i, nullptr, d.depth[level], d.vmap[level], d.nmap[level], cam, d.dmin, d.dmax, d.st, 0, 1);
 }
 
 constexpr int kBilTx = 32, kBilTy = 8, kBilMaxR = 7;
@@ -325,11 +348,9 @@ namespace {
 // `band` of the block's first nonzero depth -- block averaging with a depth-similarity
 // test, so a block straddling an occlusion edge keeps the nearer surface instead of
 // inventing a depth between the two.  Zero where the block has no depth.
-__global__ void __launch_bounds__(256) pyramid_depth_kernel(const float* __restrict__ fine, int Wf,
-                                                            float* __restrict__ coarse, int Hc, int Wc, float band)
+__device__ __forceinline__ void pyramid_depth_at(int i, const float* __restrict__ fine, int Wf,
+                                                 float* __restrict__ coarse, int Wc, float band)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= Hc * Wc) return;
     const int r = i / Wc, c = i % Wc;
     const float d[4] = {fine[(2 * r) * Wf + 2 * c], fine[(2 * r) * Wf + 2 * c + 1], fine[(2 * r + 1) * Wf + 2 * c],
                         fine[(2 * r + 1) * Wf + 2 * c + 1]};
@@ -346,16 +367,41 @@ __global__ void __launch_bounds__(256) pyramid_depth_kernel(const float* __restr
 }
 
 // the previous frame's prediction at a coarser level: the fine pixel (2i, 2j)
+__device__ __forceinline__ void pyramid_prediction_at(int i, const float4* __restrict__ pv_f,
+                                                      const float4* __restrict__ pn_f, int Wf, float4* __restrict__ pv_c,
+                                                      float4* __restrict__ pn_c, int Wc)
+{
+    const int j = (2 * (i / Wc)) * Wf + 2 * (i % Wc);
+    pv_c[i] = pv_f[j];
+    pn_c[i] = pn_f[j];
+}
+
+__global__ void __launch_bounds__(256) pyramid_depth_kernel(const float* __restrict__ fine, int Wf,
+                                                            float* __restrict__ coarse, int Hc, int Wc, float band)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < Hc * Wc) pyramid_depth_at(i, fine, Wf, coarse, Wc, band);
+}
+
 __global__ void __launch_bounds__(256) pyramid_prediction_kernel(const float4* __restrict__ pv_f,
                                                                  const float4* __restrict__ pn_f, int Wf,
                                                                  float4* __restrict__ pv_c, float4* __restrict__ pn_c,
                                                                  int Hc, int Wc)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= Hc * Wc) return;
-    const int j = (2 * (i / Wc)) * Wf + 2 * (i % Wc);
-    pv_c[i] = pv_f[j];
-    pn_c[i] = pn_f[j];
+    if (i < Hc * Wc) pyramid_prediction_at(i, pv_f, pn_f, Wf, pv_c, pn_c, Wc);
+}
+
+// level `level` of every scene's pyramid (depth and prediction) from level - 1
+__global__ void __launch_bounds__(256) pyramid_batch_kernel(const SceneDev* __restrict__ scenes, int level)
+{
+    const SceneDev& d = scenes[blockIdx.y];
+    const Camera& f = d.cam[level - 1];
+    const Camera& c = d.cam[level];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= c.H * c.W) return;
+    pyramid_depth_at(i, d.depth[level - 1], f.W, d.depth[level], c.W, d.band);
+    pyramid_prediction_at(i, d.pv[level - 1], d.pn[level - 1], f.W, d.pv[level], d.pn[level], c.W);
 }
 
 }  // namespace
@@ -369,6 +415,17 @@ void launch_pyramid_prediction(const float4* pv_f, const float4* pn_f, int Wf, f
                                int Wc, cudaStream_t s)
 {
     pyramid_prediction_kernel<<<(Hc * Wc + 255) / 256, 256, 0, s>>>(pv_f, pn_f, Wf, pv_c, pn_c, Hc, Wc);
+}
+
+void launch_pyramid_batch(const SceneDev* scenes, int n_scenes, int max_pixels, int level, cudaStream_t s)
+{
+    pyramid_batch_kernel<<<dim3((max_pixels + 255) / 256, n_scenes), 256, 0, s>>>(scenes, level);
+}
+
+void launch_vertex_batch(const SceneDev* scenes, int n_scenes, int max_pixels, int level, bool init_icp,
+                         cudaStream_t s)
+{
+    vertex_batch_kernel<<<dim3((max_pixels + 255) / 256, n_scenes), 256, 0, s>>>(scenes, level, init_icp ? 1 : 0);
 }
 
 }  // namespace kf

@@ -58,6 +58,34 @@ struct State {
     float sums[kIcpVals];  // sums of the most recent ICP iteration
 };
 
+// One scene of a batch (the batching form): the device buffers and parameters its
+// kernels need.  A batched launch covers every scene; blockIdx.y (or a flattened tile
+// index) picks the scene from a device array of these.  Level 0 aliases a handle's own
+// buffers, levels 1.. its ICP pyramid.
+constexpr int kMaxBatchLevels = 3;
+struct SceneDev {
+    Camera cam[kMaxBatchLevels];
+    Grid grid;
+    IcpParams icp;
+    const uint16_t* raw;  // this frame's depth, device
+    float* depth[kMaxBatchLevels];
+    float4* vmap[kMaxBatchLevels];
+    float4* nmap[kMaxBatchLevels];
+    float4* pv[kMaxBatchLevels];
+    float4* pn[kMaxBatchLevels];
+    float2* tab;
+    float* tsdf;
+    float* weight;
+    __half2* vol16;
+    State* st;
+    float* partials;
+    int* groups;
+    int32_t* hit;
+    long long skip_from;
+    float dmin, dmax, band;
+    int tile_start[3];  // first ray-cast tile of this scene for tile shapes 8x4, 16x2, 4x8
+};
+
 // voxel-centre coordinate, kinfu_pipeline.cpp:53-55: x * voxel_distance + voxel_distance / 2
 __device__ __forceinline__ float centre(int index, int start, float vd)
 {

@@ -375,6 +375,48 @@ __device__ __forceinline__ void add_terms(float (&v)[kIcpVals], const float (&a)
 // Group pass: one warp per 64-pixel group writes the group's 28 sums (27 terms and
 // the correspondence count) and whether the group has a correspondence.
 template <int MODE>
+__device__ __forceinline__ void group_sums(int grp, int lane, const float4* __restrict__ vmap,
+                                           const float4* __restrict__ nmap, const float4* __restrict__ pv,
+                                           const float4* __restrict__ pn, const Camera& cam, const IcpParams& prm,
+                                           const float* sF, const float* sT, float* __restrict__ partials,
+                                           int* __restrict__ flags, int32_t* __restrict__ pair)
+{
+    const int n = cam.H * cam.W;
+    float v[kIcpVals];
+#pragma unroll
+    for (int k = 0; k < kIcpVals; ++k) v[k] = 0.f;
+    for (int half = 0; half < 2; ++half) {
+        const int i = grp * 64 + half * 32 + lane;
+        if (i >= n) continue;
+        float a[6], b;
+        int j = -1;
+        const bool ok = associate(i, vmap, nmap, pv, pn, cam, sF, sT, prm.dist, prm.angle_deg, a, b, j);
+        if (MODE == 1 && pair) pair[i] = ok ? j : -1;
+        if (!ok) continue;
+        if (half == 0) {
+            add_terms(v, a, b);  // v = terms of pixel t (0 + x == x up to the sign of a zero)
+        } else {
+            float w[kIcpVals];
+#pragma unroll
+            for (int k = 0; k < kIcpVals; ++k) w[k] = 0.f;
+            add_terms(w, a, b);
+#pragma unroll
+            for (int k = 0; k < kIcpVals; ++k) v[k] = v[k] + w[k];  // sdata[t] += sdata[t + 32]
+        }
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1)
+#pragma unroll
+        for (int k = 0; k < kIcpVals; ++k) v[k] = v[k] + __shfl_down_sync(0xffffffffu, v[k], off);
+    if (lane == 0) {
+        flags[grp] = v[kIcpVals - 1] != 0.f ? 1 : 0;
+        float4* dst = reinterpret_cast<float4*>(partials + (size_t)grp * kIcpVals);
+#pragma unroll
+        for (int q = 0; q < kIcpVals / 4; ++q) dst[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+    }
+}
+
+template <int MODE>
 __global__ void __launch_bounds__(kExactWarps * 32, 4) icp_group_kernel(
     const float4* __restrict__ vmap, const float4* __restrict__ nmap, const float4* __restrict__ pv,
     const float4* __restrict__ pn, Camera cam, IcpParams prm, const float* Fsrc, const float* Tsrc,
@@ -388,41 +430,31 @@ __global__ void __launch_bounds__(kExactWarps * 32, 4) icp_group_kernel(
     }
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int n = cam.H * cam.W;
-    for (int grp = blockIdx.x * kExactWarps + warp; grp < ngroups; grp += gridDim.x * kExactWarps) {
-        float v[kIcpVals];
-#pragma unroll
-        for (int k = 0; k < kIcpVals; ++k) v[k] = 0.f;
-        for (int half = 0; half < 2; ++half) {
-            const int i = grp * 64 + half * 32 + lane;
-            if (i >= n) continue;
-            float a[6], b;
-            int j = -1;
-            const bool ok = associate(i, vmap, nmap, pv, pn, cam, sF, sT, prm.dist, prm.angle_deg, a, b, j);
-            if (MODE == 1 && pair) pair[i] = ok ? j : -1;
-            if (!ok) continue;
-            if (half == 0) {
-                add_terms(v, a, b);  // v = terms of pixel t (0 + x == x up to the sign of a zero)
-            } else {
-                float w[kIcpVals];
-#pragma unroll
-                for (int k = 0; k < kIcpVals; ++k) w[k] = 0.f;
-                add_terms(w, a, b);
-#pragma unroll
-                for (int k = 0; k < kIcpVals; ++k) v[k] = v[k] + w[k];  // sdata[t] += sdata[t + 32]
-            }
-        }
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1)
-#pragma unroll
-            for (int k = 0; k < kIcpVals; ++k) v[k] = v[k] + __shfl_down_sync(0xffffffffu, v[k], off);
-        if (lane == 0) {
-            flags[grp] = v[kIcpVals - 1] != 0.f ? 1 : 0;
-            float4* dst = reinterpret_cast<float4*>(partials + (size_t)grp * kIcpVals);
-#pragma unroll
-            for (int q = 0; q < kIcpVals / 4; ++q) dst[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
-        }
+    for (int grp = blockIdx.x * kExactWarps + warp; grp < ngroups; grp += gridDim.x * kExactWarps)
+        group_sums<MODE>(grp, lane, vmap, nmap, pv, pn, cam, prm, sF, sT, partials, flags, pair);
+}
+
+// the group pass of every scene of a batch at pyramid level `level`; WARPS warps per
+// block (a shape the batch's autotuner picks)
+template <int WARPS>
+__global__ void __launch_bounds__(WARPS * 32) icp_group_batch_kernel(const SceneDev* __restrict__ scenes, int level)
+{
+    wait_for_producer();
+    const SceneDev& d = scenes[blockIdx.y];
+    const Camera& cam = d.cam[level];
+    const int ngroups = (cam.H * cam.W + 63) / 64;
+    if ((int)blockIdx.x * WARPS >= ngroups) return;
+    __shared__ float sF[16], sT[16];
+    if (threadIdx.x < 16) {
+        sF[threadIdx.x] = d.st->F[threadIdx.x];
+        sT[threadIdx.x] = d.st->T[threadIdx.x];
     }
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int grp = blockIdx.x * WARPS + warp;
+    if (grp < ngroups)
+        group_sums<0>(grp, lane, d.vmap[level], d.nmap[level], d.pv[level], d.pn[level], cam, d.icp, sF, sT,
+                      d.partials, d.groups, nullptr);
 }
 
 // Reduce-and-solve pass: one warp.  The group sums are streamed into shared memory in
@@ -470,10 +502,9 @@ __device__ __forceinline__ bool bar_wait(unsigned long long* bar, unsigned parit
 }
 
 template <int MODE>
-__global__ void __launch_bounds__(32, 1) icp_solve_kernel(const float* __restrict__ partials, int ngroups, State* st,
-                                                        IcpParams prm, float* sums_out)
+__device__ __forceinline__ void solve_body(const float* __restrict__ partials, int ngroups, State* st,
+                                           const IcpParams& prm, float* sums_out)
 {
-    wait_for_producer();
     extern __shared__ float4 smem4[];
     float* buf = reinterpret_cast<float*>(smem4);  // kBuffers x kChunkGroups x kIcpVals
     __shared__ __align__(8) unsigned long long bars[kBuffers];
@@ -741,6 +772,23 @@ __global__ void __launch_bounds__(kExactWarps * 32, 4) icp_precise_kernel(
     finish_precise_warp(st, prm, red_hi, red_lo);
 }
 
+template <int MODE>
+__global__ void __launch_bounds__(32, 1) icp_solve_kernel(const float* __restrict__ partials, int ngroups, State* st,
+                                                        IcpParams prm, float* sums_out)
+{
+    wait_for_producer();
+    solve_body<MODE>(partials, ngroups, st, prm, sums_out);
+}
+
+// every scene's reduce-and-solve pass: one one-warp CTA per scene, all at once
+__global__ void __launch_bounds__(32, 1) icp_solve_batch_kernel(const SceneDev* __restrict__ scenes, int level)
+{
+    wait_for_producer();
+    const SceneDev& d = scenes[blockIdx.x];
+    const Camera& cam = d.cam[level];
+    solve_body<0>(d.partials, (cam.H * cam.W + 63) / 64, d.st, d.icp, nullptr);
+}
+
 size_t solve_smem_bytes(int /*ngroups*/) { return (size_t)kBuffers * kChunkBytes; }
 
 // the reduce-and-solve warp needs more than the default 48 KB of dynamic shared memory
@@ -753,6 +801,7 @@ void ensure_solve_smem(int ngroups)
     if (dev < 0 || dev >= 64 || configured[dev] >= need) return;
     cudaFuncSetAttribute(icp_solve_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, need);
     cudaFuncSetAttribute(icp_solve_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, need);
+    cudaFuncSetAttribute(icp_solve_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, need);
     configured[dev] = need;
 }
 
@@ -831,6 +880,39 @@ void launch_icp_associate(const float4* vmap, const float4* nmap, const float4* 
     } else
         icp_kernel<false, 1><<<blocks, kIcpBlock, 0, s>>>(vmap, nmap, pv, pn, cam, prm, st, F, T, partials,
                                                           sums_out, pair);
+}
+
+void launch_icp_iteration_batch(const SceneDev* scenes, int n_scenes, int max_groups, int level, int warps,
+                                cudaStream_t s)
+{
+    ensure_solve_smem(max_groups);
+    switch (warps) {
+    case 4:
+        launch_pdl(icp_group_batch_kernel<4>, dim3((max_groups + 3) / 4, n_scenes), dim3(4 * 32), 0, s, scenes, level);
+        break;
+    case 16:
+        launch_pdl(icp_group_batch_kernel<16>, dim3((max_groups + 15) / 16, n_scenes), dim3(16 * 32), 0, s, scenes,
+                   level);
+        break;
+    default:
+        launch_pdl(icp_group_batch_kernel<8>, dim3((max_groups + 7) / 8, n_scenes), dim3(8 * 32), 0, s, scenes, level);
+    }
+    launch_pdl(icp_solve_batch_kernel, dim3(n_scenes), dim3(32), solve_smem_bytes(max_groups), s, scenes, level);
+}
+
+void launch_icp_group_batch(const SceneDev* scenes, int n_scenes, int max_groups, int level, int warps, cudaStream_t s)
+{
+    switch (warps) {
+    case 4:
+        launch_pdl(icp_group_batch_kernel<4>, dim3((max_groups + 3) / 4, n_scenes), dim3(4 * 32), 0, s, scenes, level);
+        break;
+    case 16:
+        launch_pdl(icp_group_batch_kernel<16>, dim3((max_groups + 15) / 16, n_scenes), dim3(16 * 32), 0, s, scenes,
+                   level);
+        break;
+    default:
+        launch_pdl(icp_group_batch_kernel<8>, dim3((max_groups + 7) / 8, n_scenes), dim3(8 * 32), 0, s, scenes, level);
+    }
 }
 
 }  // namespace kf

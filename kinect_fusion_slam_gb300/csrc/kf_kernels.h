@@ -68,6 +68,30 @@ void launch_calibrate(State* st, cudaStream_t s);
 void launch_pyramid_depth(const float* fine, int Wf, float* coarse, int Hc, int Wc, float band, cudaStream_t s);
 void launch_pyramid_prediction(const float4* pv_f, const float4* pn_f, int Wf, float4* pv_c, float4* pn_c, int Hc,
                                int Wc, cudaStream_t s);
+
+// ---- the batching form: one launch per stage over a device array of scenes ----------
+// max_pixels / max_blocks: the largest scene's count at that level (smaller scenes' extra
+// blocks return at once)
+void launch_vertex_batch(const SceneDev* scenes, int n_scenes, int max_pixels, int level, bool init_icp,
+                         cudaStream_t s);
+void launch_pyramid_batch(const SceneDev* scenes, int n_scenes, int max_pixels, int level, cudaStream_t s);
+// one ICP iteration of every scene at `level` in the reference summation order: the
+// group pass (warps per block: 4, 8 or 16) and one one-warp solve CTA per scene;
+// max_groups: the largest scene's 64-pixel groups at that level
+void launch_icp_iteration_batch(const SceneDev* scenes, int n_scenes, int max_groups, int level, int warps,
+                                cudaStream_t s);
+// every scene's integration prep + integration (z chunks of zchunk voxels); max_tiles:
+// the largest integrate_tiles() over the scenes
+void launch_integrate_batch(const SceneDev* scenes, int n_scenes, int max_pixels, int max_tiles, int zchunk, bool f16,
+                            bool first, cudaStream_t s);
+int integrate_tiles(const Grid& g, int zchunk);
+// every scene's ray cast, persistent over all scenes' tiles; shape 0: 8x4, 1: 16x2,
+// 2: 4x8 pixels per warp tile; tile_counter: two device unsigneds, zero between launches
+int raycast_tiles(int H, int W, int shape);
+void launch_raycast_batch(const SceneDev* scenes, int n_scenes, unsigned total_tiles, bool f16, int shape,
+                          int blocks, unsigned* tile_counter, cudaStream_t s);
+// the group pass alone (idempotent: what the autotuner times)
+void launch_icp_group_batch(const SceneDev* scenes, int n_scenes, int max_groups, int level, int warps, cudaStream_t s);
 // packs the predicted points with z != 0 into out (2 float4 per point, unordered) and
 // counts them into *count (zero on entry)
 void launch_compact_cloud(const float4* pv, const float4* pn, int n, float4* out, unsigned* count, cudaStream_t s);

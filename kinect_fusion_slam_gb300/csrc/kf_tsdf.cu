@@ -67,11 +67,9 @@ struct ViewF16 {
 // only on the pixel and the pose.  tab = (predicted_depth or NaN where the depth is
 // 0, 1 / |ray direction|).  Thread 0 also stores T^-1 (cv::Mat::inv, :149) and the
 // in-front axis (:57-71).
-__global__ void __launch_bounds__(256) integrate_prep_kernel(const float* __restrict__ depth, float2* __restrict__ tab,
-                                                             Camera cam, State* st)
+__device__ __forceinline__ void integrate_prep_at(int i, const float* __restrict__ depth, float2* __restrict__ tab,
+                                                  const Camera& cam, State* st)
 {
-    wait_for_producer();
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const float* K = cam.K;
     const float* Ki = cam.Ki;
     float T[16];
@@ -107,19 +105,32 @@ __global__ void __launch_bounds__(256) integrate_prep_kernel(const float* __rest
     tab[i] = make_float2(D != 0 ? pd : qnan(), 1.f / mag);
 }
 
+__global__ void __launch_bounds__(256) integrate_prep_kernel(const float* __restrict__ depth, float2* __restrict__ tab,
+                                                             Camera cam, State* st)
+{
+    wait_for_producer();
+    integrate_prep_at(blockIdx.x * blockDim.x + threadIdx.x, depth, tab, cam, st);
+}
+
+__global__ void __launch_bounds__(256) integrate_prep_batch_kernel(const SceneDev* __restrict__ scenes)
+{
+    wait_for_producer();
+    const SceneDev& d = scenes[blockIdx.y];
+    integrate_prep_at(blockIdx.x * blockDim.x + threadIdx.x, d.depth[0], d.tab, d.cam[0], d.st);
+}
+
 constexpr int kIntTx = 32, kIntTy = 8;
 
 template <class Vol, bool FIRST>
-__global__ void __launch_bounds__(kIntTx* kIntTy) integrate_kernel(Vol vol, const float2* __restrict__ tab,
-                                                                   const State* __restrict__ st, Grid g, float fx,
-                                                                   float fy, float cx, float cy, int H, int W,
-                                                                   int zchunk, long long skip_from)
+__device__ __forceinline__ void integrate_at(const Vol& vol, const float2* __restrict__ tab,
+                                             const State* __restrict__ st, const Grid& g, float fx, float fy, float cx,
+                                             float cy, int H, int W, int zchunk, long long skip_from, int bx, int by,
+                                             int bz)
 {
-    wait_for_producer();
-    const int x = blockIdx.x * kIntTx + threadIdx.x;
-    const int y = blockIdx.y * kIntTy + threadIdx.y;
+    const int x = bx * kIntTx + threadIdx.x;
+    const int y = by * kIntTy + threadIdx.y;
     if (x >= g.dx || y >= g.dy) return;
-    const int z0 = blockIdx.z * zchunk;
+    const int z0 = bz * zchunk;
     const int z1 = min(z0 + zchunk, g.dz);
     float ti[12];
 #pragma unroll
@@ -216,6 +227,37 @@ __global__ void __launch_bounds__(kIntTx* kIntTy) integrate_kernel(Vol vol, cons
             vol.store(lin, (w * t + 1.0f * f) / (w + 1.0f), w + 1.0f);
         }
     }
+}
+
+template <class Vol, bool FIRST>
+__global__ void __launch_bounds__(kIntTx* kIntTy) integrate_kernel(Vol vol, const float2* __restrict__ tab,
+                                                                   const State* __restrict__ st, Grid g, float fx,
+                                                                   float fy, float cx, float cy, int H, int W,
+                                                                   int zchunk, long long skip_from)
+{
+    wait_for_producer();
+    integrate_at<Vol, FIRST>(vol, tab, st, g, fx, fy, cx, cy, H, W, zchunk, skip_from, blockIdx.x, blockIdx.y,
+                             blockIdx.z);
+}
+
+__device__ __forceinline__ VolF32 scene_volume(const SceneDev& d, VolF32*) { return VolF32{d.tsdf, d.weight}; }
+__device__ __forceinline__ VolF16 scene_volume(const SceneDev& d, VolF16*) { return VolF16{d.vol16}; }
+
+// every scene's integration: blockIdx.y picks the scene, blockIdx.x its (x, y, z-chunk)
+// tile; scenes with fewer tiles than the largest return early
+template <class Vol, bool FIRST>
+__global__ void __launch_bounds__(kIntTx* kIntTy) integrate_batch_kernel(const SceneDev* __restrict__ scenes, int zchunk)
+{
+    wait_for_producer();
+    const SceneDev& d = scenes[blockIdx.y];
+    const Grid& g = d.grid;
+    const int nbx = (g.dx + kIntTx - 1) / kIntTx, nby = (g.dy + kIntTy - 1) / kIntTy, nbz = (g.dz + zchunk - 1) / zchunk;
+    const int t = blockIdx.x;
+    if (t >= nbx * nby * nbz) return;
+    const Camera& cam = d.cam[0];
+    const Vol vol = scene_volume(d, (Vol*)nullptr);
+    integrate_at<Vol, FIRST>(vol, d.tab, d.st, g, cam.K[0], cam.K[4], cam.K[2], cam.K[5], cam.H, cam.W, zchunk,
+                             d.skip_from, t % nbx, (t / nbx) % nby, t / (nbx * nby));
 }
 
 // Ray_Box_Intersection, voxel_traversal.cu:4-73
@@ -514,6 +556,58 @@ __global__ void __launch_bounds__(kRayBlock, 4) raycast_kernel(View vol, const f
     }
 }
 
+__device__ __forceinline__ ViewF32 scene_view(const SceneDev& d, ViewF32*) { return ViewF32{d.tsdf}; }
+__device__ __forceinline__ ViewF16 scene_view(const SceneDev& d, ViewF16*) { return ViewF16{d.vol16}; }
+
+// Every scene's ray cast in one persistent launch: warps take TW x (32/TW)-pixel tiles
+// from one counter over all scenes' tiles (scene s owns tiles [tile_start[shape],
+// tile_start[shape] of s + 1)), so uneven scenes share the SMs without a tail per scene.
+template <class View, int TW, int SHAPE>
+__global__ void __launch_bounds__(kRayBlock, 4) raycast_batch_kernel(const SceneDev* __restrict__ scenes, int n_scenes,
+                                                                  unsigned total_tiles, unsigned* tile_counter)
+{
+    wait_for_producer();
+    constexpr int TH = 32 / TW;
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        unsigned tile = 0;
+        if (lane == 0) tile = atomicAdd(tile_counter, 1u);
+        tile = __shfl_sync(0xffffffffu, tile, 0);
+        if (tile >= total_tiles) {
+            if (lane == 0) {
+                const unsigned warps = gridDim.x * (blockDim.x / 32);
+                if (atomicAdd(tile_counter + 1, 1u) == warps - 1) {
+                    tile_counter[0] = 0u;
+                    tile_counter[1] = 0u;
+                }
+            }
+            return;
+        }
+        int s = 0;
+        while (s + 1 < n_scenes && tile >= (unsigned)scenes[s + 1].tile_start[SHAPE]) ++s;
+        const SceneDev& d = scenes[s];
+        const Camera& cam = d.cam[0];
+        const unsigned t = tile - (unsigned)d.tile_start[SHAPE];
+        const int tiles_x = (cam.W + TW - 1) / TW;
+        const int px = (int)(t % tiles_x) * TW + (lane % TW);
+        const int py = (int)(t / tiles_x) * TH + lane / TW;
+        if (px >= cam.W || py >= cam.H) continue;
+        float T[12];
+#pragma unroll
+        for (int k = 0; k < 12; ++k) T[k] = d.st->T[k];
+        const int i = py * cam.W + px;
+        float4 op = make_float4(0.f, 0.f, 0.f, 0.f), on = op;
+        int oh = -1;
+        const float D = d.depth[0][i];
+        if (D != 0)
+            trace(scene_view(d, (View*)nullptr), (float)px + 1.0f, (float)py + 1.0f, D, cam.Ki, T, d.grid,
+                  d.st->c_flip, op, on, oh);
+        d.pv[0][i] = op;
+        d.pn[0][i] = on;
+        if (d.hit) d.hit[i] = oh;
+    }
+}
+
 }  // namespace
 
 int raycast_blocks()
@@ -580,6 +674,59 @@ void launch_raycast_f16(const __half2* vol, const float* depth, float4* pv, floa
 {
     launch_pdl(raycast_kernel<ViewF16>, dim3(raycast_blocks()), dim3(kRayBlock), 0, s, ViewF16{vol}, depth, pv, pn,
                hit, cam, g, st, tile_counter);
+}
+
+void launch_integrate_batch(const SceneDev* scenes, int n_scenes, int max_pixels, int max_tiles, int zchunk, bool f16,
+                            bool first, cudaStream_t s)
+{
+    launch_pdl(integrate_prep_batch_kernel, dim3((max_pixels + 255) / 256, n_scenes), dim3(256), 0, s, scenes);
+    const dim3 grid(max_tiles, n_scenes), block(kIntTx, kIntTy);
+    if (f16) {
+        if (first)
+            launch_pdl(integrate_batch_kernel<VolF16, true>, grid, block, 0, s, scenes, zchunk);
+        else
+            launch_pdl(integrate_batch_kernel<VolF16, false>, grid, block, 0, s, scenes, zchunk);
+    } else {
+        if (first)
+            launch_pdl(integrate_batch_kernel<VolF32, true>, grid, block, 0, s, scenes, zchunk);
+        else
+            launch_pdl(integrate_batch_kernel<VolF32, false>, grid, block, 0, s, scenes, zchunk);
+    }
+}
+
+int integrate_tiles(const Grid& g, int zchunk)
+{
+    return ((g.dx + kIntTx - 1) / kIntTx) * ((g.dy + kIntTy - 1) / kIntTy) * ((g.dz + zchunk - 1) / zchunk);
+}
+
+int raycast_tiles(int H, int W, int shape)
+{
+    const int tw = shape == 1 ? 16 : (shape == 2 ? 4 : 8), th = 32 / tw;
+    return ((W + tw - 1) / tw) * ((H + th - 1) / th);
+}
+
+void launch_raycast_batch(const SceneDev* scenes, int n_scenes, unsigned total_tiles, bool f16, int shape,
+                          int blocks, unsigned* tile_counter, cudaStream_t s)
+{
+    const dim3 grid(blocks), block(kRayBlock);
+#define KF_RAY_BATCH(VIEW, TW, SH) \
+    launch_pdl(raycast_batch_kernel<VIEW, TW, SH>, grid, block, 0, s, scenes, n_scenes, total_tiles, tile_counter)
+    if (f16) {
+        if (shape == 1)
+            KF_RAY_BATCH(ViewF16, 16, 1);
+        else if (shape == 2)
+            KF_RAY_BATCH(ViewF16, 4, 2);
+        else
+            KF_RAY_BATCH(ViewF16, 8, 0);
+    } else {
+        if (shape == 1)
+            KF_RAY_BATCH(ViewF32, 16, 1);
+        else if (shape == 2)
+            KF_RAY_BATCH(ViewF32, 4, 2);
+        else
+            KF_RAY_BATCH(ViewF32, 8, 0);
+    }
+#undef KF_RAY_BATCH
 }
 
 }  // namespace kf
