@@ -56,6 +56,8 @@ def parse_args(argv=None):
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-ate", action="store_true", help="skip the trajectory comparison with the FP64 oracle")
+    p.add_argument("--no-extra-forms", action="store_true", help="skip the batching (c4) and differentiation (c3) runs")
+    p.add_argument("--batch-frames", type=int, default=20, help="timed frames of the batching run")
     return p.parse_args(argv)
 
 
@@ -422,6 +424,111 @@ def roofline_of(cfg, r, form: str):
                        for k, v in stages.items()}}
 
 
+def run_batching(args, stream) -> dict:
+    """The batching form on c4: 16 scenes of uneven grids (128^3 @ 20 mm, 256^3 @ 15 mm,
+    384x384x320 @ 10 mm) and depth sizes (640x480, 320x240), BATCH_FRAMES rendered
+    frames each played forwards and back; scene-frames/s of the batch (every stage one
+    launch over all scenes, one graph per frame) against the same scenes run one after
+    another on their own handles."""
+    import torch
+
+    import kinect_fusion_slam_gb300 as kf
+    from kinect_fusion_slam_gb300 import scene
+
+    cfgs = scene.batch_configs(16)
+    unique = 4
+    seqs = [scene.sequence(c, frames=unique) for c in cfgs]
+    depths = [torch.from_numpy(sq.depths(unique).view(np.int16)).cuda() for sq in seqs]
+    confs = [kf.make_config(height=c.camera.height, width=c.camera.width, dims=c.grid.dims, grid_start=c.grid.start,
+                            voxel_size=c.grid.voxel_size) for c in cfgs]
+    fbytes = [c.camera.height * c.camera.width * 2 for c in cfgs]
+    steps = args.batch_frames
+    order = pingpong(unique, 1 + args.warmup + steps)
+
+    def ptrs(k):
+        return [d.data_ptr() + order[k] * n for d, n in zip(depths, fbytes)]
+
+    b = kf.Batch(confs)
+    for h, sq in zip(b.scenes, seqs):
+        h.set_intrinsics(sq.K[0, 0], sq.K[1, 1], sq.K[0, 2], sq.K[1, 2])
+    b.initial_processing_device(ptrs(0))
+    b.synchronize()
+    tuning = b.autotune()
+    for k in range(1, 1 + args.warmup):
+        b.incoming_frame_device(ptrs(k))
+    b.synchronize()
+    t0 = time.perf_counter()
+    for k in range(1 + args.warmup, 1 + args.warmup + steps):
+        b.incoming_frame_device(ptrs(k))
+    b.synchronize()
+    t_batch = time.perf_counter() - t0
+    kpf = b.kernels_per_frame()
+    b.close()
+
+    singles = [kf.Handle(c) for c in confs]
+    for h, sq in zip(singles, seqs):
+        h.set_intrinsics(sq.K[0, 0], sq.K[1, 1], sq.K[0, 2], sq.K[1, 2])
+        h.set_stream(stream.cuda_stream)
+    for h, p in zip(singles, ptrs(0)):
+        h.initial_processing_device(p)
+    for k in range(1, 1 + args.warmup):
+        for h, p in zip(singles, ptrs(k)):
+            h.incoming_frame_device(p)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for k in range(1 + args.warmup, 1 + args.warmup + steps):
+        for h, p in zip(singles, ptrs(k)):
+            h.incoming_frame_device(p)
+    torch.cuda.synchronize()
+    t_single = time.perf_counter() - t0
+    for h in singles:
+        h.close()
+    n = len(cfgs)
+    return {"workload": "c4: 16 scenes, grids 128^3 @ 20 mm / 256^3 @ 15 mm / 384x384x320 @ 10 mm, "
+                        "640x480 and 320x240 depth, single-level ICP x10",
+            "scene_frames_per_s": n * steps / t_batch, "scene_frames_per_s_one_by_one": n * steps / t_single,
+            "speedup": t_single / t_batch, "frames": steps, "kernels_per_batch_frame": kpf,
+            "tuning": {"icp_group_warps": tuning[0], "ray_tile": ["8x4", "16x2", "4x8"][tuning[1]],
+                       "ray_blocks_per_sm": tuning[2], "integration_z_chunk": tuning[3]}}
+
+
+def run_differentiation(args) -> dict:
+    """The differentiation form on c3: a 256^3 TSDF at 10 mm (an analytic room with a
+    sphere), 64 poses; device time per 640x480 trilinear render and per adjoint
+    (voxel + pose gradients), CUDA events on the current stream."""
+    import torch
+
+    from kinect_fusion_slam_gb300 import diff, scene
+
+    cfg = scene.config("c3")
+    g = cfg.grid
+    idx = [torch.arange(n, dtype=torch.float32, device="cuda") for n in g.dims]
+    x, y, z = [(idx[k] + g.start[k] + 0.5) * g.voxel_size for k in range(3)]
+    Z, Y, X = torch.meshgrid(z, y, x, indexing="ij")
+    sdf = torch.minimum(torch.sqrt(X ** 2 + Y ** 2 + (Z - 1200.0) ** 2) - 350.0, 2000.0 - Z)
+    sdf = torch.minimum(sdf, 900.0 - Y)
+    tsdf = torch.clamp(sdf / 100.0, -1.0, 1.0).contiguous()
+    K = cfg.camera.K_reference()
+    d = diff.make_desc(cfg.camera.height, cfg.camera.width, K, g.dims, g.start, g.voxel_size, 300.0, 2500.0)
+    poses = [diff.se3_exp([0.002 * k, -0.001 * k, 0.0015 * k, 2.0 * k, -1.0 * k, 3.0 * k]) for k in range(64)]
+    gD = torch.ones(cfg.camera.height, cfg.camera.width, device="cuda")
+    e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    for T in poses[:3]:
+        diff.render(d, tsdf, T)
+        diff.render_backward(d, tsdf, T, gD, None)
+    torch.cuda.synchronize()
+    e[0].record()
+    for T in poses:
+        diff.render(d, tsdf, T)
+    e[1].record()
+    for T in poses:
+        diff.render_backward(d, tsdf, T, gD, None)
+    e[2].record()
+    torch.cuda.synchronize()
+    return {"workload": "c3: 256^3 TSDF @ 10 mm, 640x480 render, 64 poses",
+            "render_ms": e[0].elapsed_time(e[1]) / len(poses), "adjoint_ms": e[1].elapsed_time(e[2]) / len(poses)}
+
+
 def run_gb300(args, dist: Dist):
     import torch
 
@@ -441,6 +548,11 @@ def run_gb300(args, dist: Dist):
     forms = ["precision", "plain"] if args.form == "both" else [args.form]
     res = {f: run_form(args, dist, f, cfg, frames, order, fresh, stream) for f in forms}
     head = res[forms[0]]
+
+    extra = {}
+    if not args.no_extra_forms and dist.world == 1:
+        extra["batching_c4"] = run_batching(args, stream)
+        extra["differentiation_c3"] = run_differentiation(args)
 
     cb = None
     if dist.rank == 0 and args.gpus == 1 and not args.no_cpu_baseline:
@@ -466,6 +578,7 @@ def run_gb300(args, dist: Dist):
                              "roofline": roofline_of(cfg, p, "plain")}
         line["speedup_vs_fp32_form"] = head["value"] / p["value"]
         line["gpu_launches"] = head["gpu_launches"] + p["gpu_launches"]
+    line.update(extra)
     if dist.rank == 0:
         print(json.dumps(line), flush=True)
     dist.close()
