@@ -73,30 +73,33 @@ struct Acc {
     }
 };
 
-__device__ __forceinline__ bool associate(int i, const float4* __restrict__ vmap, const float4* __restrict__ nmap,
-                                          const float4* __restrict__ pv, const float4* __restrict__ pn,
-                                          const Camera& cam, const float* F, const float* T, float dist_th,
-                                          float ang_th, float (&a)[6], float& b, int& j)
+// sensor_pose_estimation.cu:20-48, first half: the vertex (vmap.w holds the vertex mask),
+// its projection through F and K (the reference projects through K although its kernel
+// argument is named dev_inv_cam_intrinsic: the launch at :353 passes dev_cam_intrinsic)
+// and, when it lands in the image, the matched pixel j and the vertex in world g
+__device__ __forceinline__ bool assoc_project(float4 v, const Camera& cam, const float* F, const float* T, float3& g,
+                                              int& j)
 {
-    const float4 v = vmap[i];
-    // sensor_pose_estimation.cu:20 (vmap.w holds the vertex mask)
     if (!(v.z != 0 && v.w != 0)) return false;
     const float3 p3 = make_float3(v.x, v.y, v.z);
     const float3 c = xform(F, p3);
-    // the reference projects through K (its kernel argument named dev_inv_cam_intrinsic
-    // receives dev_cam_intrinsic at :353)
     const float3 p = mul3(cam.K, c);
     const int u = (int)roundf(p.x / p.z);
     const int vv = (int)roundf(p.y / p.z);
     if (!(u > 0 && u <= cam.W && vv > 0 && vv <= cam.H)) return false;
-    const float3 g = xform(T, p3);
+    g = xform(T, p3);
     j = (vv - 1) * cam.W + (u - 1);
-    const float4 q = pv[j];
-    const float4 m = pn[j];
+    return true;
+}
+
+// second half (:44-131): the distance and normal-angle gates against the prediction
+// (q, m) at j, then the row a and residual b
+__device__ __forceinline__ bool assoc_finish(float3 g, float4 n, float4 q, float4 m, const float* T, float dist_th,
+                                             float ang_th, float (&a)[6], float& b)
+{
     const float3 dd = make_float3(g.x - q.x, g.y - q.y, g.z - q.z);
     const float dist = sqrtf(dd.x * dd.x + dd.y * dd.y + dd.z * dd.z);
     if (!(dist <= dist_th && dist >= 0.0f)) return false;
-    const float4 n = nmap[i];
     const float3 un = normalized(make_float3(T[0] * n.x + T[1] * n.y + T[2] * n.z, T[4] * n.x + T[5] * n.y + T[6] * n.z,
                                              T[8] * n.x + T[9] * n.y + T[10] * n.z));
     const float3 va = normalized(make_float3(m.x, m.y, m.z));
@@ -111,6 +114,52 @@ __device__ __forceinline__ bool associate(int i, const float4* __restrict__ vmap
     a[5] = m.z;
     b = m.x * (q.x - g.x) + m.y * (q.y - g.y) + m.z * (q.z - g.z);
     return true;
+}
+
+__device__ __forceinline__ bool associate(int i, const float4* __restrict__ vmap, const float4* __restrict__ nmap,
+                                          const float4* __restrict__ pv, const float4* __restrict__ pn,
+                                          const Camera& cam, const float* F, const float* T, float dist_th,
+                                          float ang_th, float (&a)[6], float& b, int& j)
+{
+    float3 g;
+    if (!assoc_project(vmap[i], cam, F, T, g, j)) return false;
+    return assoc_finish(g, nmap[i], pv[j], pn[j], T, dist_th, ang_th, a, b);
+}
+
+// The same for a lane's two pixels of a 64-pixel group (i and i + 32), arranged so
+// that each round of loads is issued for both pixels before either is used -- the
+// vertices and normals together, then both matched predictions -- which turns six
+// dependent L2 round trips into two.  The arithmetic is associate()'s, operation for
+// operation; only independent loads move.
+__device__ __forceinline__ void associate_pair(int i0, int n, const float4* __restrict__ vmap,
+                                               const float4* __restrict__ nmap, const float4* __restrict__ pv,
+                                               const float4* __restrict__ pn, const Camera& cam, const float* F,
+                                               const float* T, float dist_th, float ang_th, bool (&ok)[2],
+                                               float (&a)[2][6], float (&b)[2], int (&j)[2])
+{
+    const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 v[2], nn[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const int i = i0 + 32 * h;
+        v[h] = i < n ? vmap[i] : zero;
+        nn[h] = i < n ? nmap[i] : zero;
+    }
+    float3 g[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        j[h] = -1;
+        ok[h] = assoc_project(v[h], cam, F, T, g[h], j[h]);
+    }
+    float4 q[2], m[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        q[h] = ok[h] ? pv[j[h]] : zero;
+        m[h] = ok[h] ? pn[j[h]] : zero;
+    }
+#pragma unroll
+    for (int h = 0; h < 2; ++h)
+        if (ok[h]) ok[h] = assoc_finish(g[h], nn[h], q[h], m[h], T, dist_th, ang_th, a[h], b[h]);
 }
 
 // Deterministic block reduction: butterfly shuffles within each warp, then warp
@@ -385,24 +434,22 @@ __device__ __forceinline__ void group_sums(int grp, int lane, const float4* __re
     float v[kIcpVals];
 #pragma unroll
     for (int k = 0; k < kIcpVals; ++k) v[k] = 0.f;
-    for (int half = 0; half < 2; ++half) {
-        const int i = grp * 64 + half * 32 + lane;
-        if (i >= n) continue;
-        float a[6], b;
-        int j = -1;
-        const bool ok = associate(i, vmap, nmap, pv, pn, cam, sF, sT, prm.dist, prm.angle_deg, a, b, j);
-        if (MODE == 1 && pair) pair[i] = ok ? j : -1;
-        if (!ok) continue;
-        if (half == 0) {
-            add_terms(v, a, b);  // v = terms of pixel t (0 + x == x up to the sign of a zero)
-        } else {
-            float w[kIcpVals];
+    bool ok[2];
+    float a[2][6], b[2];
+    int j[2];
+    associate_pair(grp * 64 + lane, n, vmap, nmap, pv, pn, cam, sF, sT, prm.dist, prm.angle_deg, ok, a, b, j);
+    if (MODE == 1 && pair) {
+        if (grp * 64 + lane < n) pair[grp * 64 + lane] = ok[0] ? j[0] : -1;
+        if (grp * 64 + 32 + lane < n) pair[grp * 64 + 32 + lane] = ok[1] ? j[1] : -1;
+    }
+    if (ok[0]) add_terms(v, a[0], b[0]);  // v = terms of pixel t (0 + x == x up to the sign of a zero)
+    if (ok[1]) {
+        float w[kIcpVals];
 #pragma unroll
-            for (int k = 0; k < kIcpVals; ++k) w[k] = 0.f;
-            add_terms(w, a, b);
+        for (int k = 0; k < kIcpVals; ++k) w[k] = 0.f;
+        add_terms(w, a[1], b[1]);
 #pragma unroll
-            for (int k = 0; k < kIcpVals; ++k) v[k] = v[k] + w[k];  // sdata[t] += sdata[t + 32]
-        }
+        for (int k = 0; k < kIcpVals; ++k) v[k] = v[k] + w[k];  // sdata[t] += sdata[t + 32]
     }
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1)
@@ -707,15 +754,16 @@ __global__ void __launch_bounds__(kExactWarps * 32, 4) icp_precise_kernel(
 #pragma unroll
     for (int k = 0; k < kIcpVals; ++k) v[k] = 0.f;
     if (grp < ngroups) {
-        for (int half = 0; half < 2; ++half) {
-            const int i = grp * 64 + half * 32 + lane;
-            if (i >= n) continue;
-            float a[6], b;
-            int j = -1;
-            const bool ok = associate(i, vmap, nmap, pv, pn, cam, sF, sT, prm.dist, prm.angle_deg, a, b, j);
-            if (MODE == 1 && pair) pair[i] = ok ? j : -1;
-            if (ok) add_terms(v, a, b);
+        bool ok[2];
+        float a[2][6], b[2];
+        int j[2];
+        associate_pair(grp * 64 + lane, n, vmap, nmap, pv, pn, cam, sF, sT, prm.dist, prm.angle_deg, ok, a, b, j);
+        if (MODE == 1 && pair) {
+            if (grp * 64 + lane < n) pair[grp * 64 + lane] = ok[0] ? j[0] : -1;
+            if (grp * 64 + 32 + lane < n) pair[grp * 64 + 32 + lane] = ok[1] ? j[1] : -1;
         }
+        if (ok[0]) add_terms(v, a[0], b[0]);
+        if (ok[1]) add_terms(v, a[1], b[1]);
 #pragma unroll
         for (int off = 16; off > 0; off >>= 1)
 #pragma unroll

@@ -385,13 +385,17 @@ __device__ __forceinline__ void trace(const View& vol, float X, float Y, float D
         bz = !(bx || by);
     };
     // The stepping never depends on the loaded values, only the termination does, so a
-    // lead walker with the same arithmetic runs kAhead steps in front and issues the
-    // loads early into a register ring; the trailing walk consumes them in order.  The
-    // lead loads only voxels inside the loop bounds.
+    // lead walker with the same arithmetic runs kAhead steps in front: at each position
+    // it issues the voxel's load into a register ring and records, beside it, whether
+    // the position is inside the loop bounds and which axis the step from it takes.  The
+    // trailing walk consumes value, flag and axis in order, so it repeats neither the
+    // bounds test nor the t_max comparisons.  The lead loads only voxels inside the
+    // bounds.
     constexpr int kAhead = 4;
     int ax = ix, ay = iy, az = iz, ali = li;
     float3 atm = tm;
-    auto lead_step = [&]() {
+    // one Amanatides-Woo step of the lead; returns the axis (0 x, 1 y, 2 z)
+    auto lead_step = [&]() -> int {
         bool bx, by, bz;
         pick(atm, bx, by, bz);
         ax += bx ? sx : 0;
@@ -402,12 +406,15 @@ __device__ __forceinline__ void trace(const View& vol, float X, float Y, float D
         atm.x = bx ? nx : atm.x;
         atm.y = by ? ny : atm.y;
         atm.z = bz ? nz : atm.z;
+        return bx ? 0 : (by ? 1 : 2);
     };
     typename View::Raw ring[kAhead];
+    int code[kAhead];  // 4: inside the bounds, | axis of the step
 #pragma unroll
     for (int k = 0; k < kAhead; ++k) {
-        ring[k] = inside_grid(ax, ay, az) ? vol.raw(ali) : typename View::Raw(0);
-        lead_step();
+        const bool in = inside_grid(ax, ay, az);
+        ring[k] = in ? vol.raw(ali) : typename View::Raw(0);
+        code[k] = (in ? 4 : 0) | lead_step();
     }
     float prev = 0.0f;
     float crossing = 0.f;  // the negative value met right after a positive one, or 0
@@ -417,13 +424,15 @@ __device__ __forceinline__ void trace(const View& vol, float X, float Y, float D
     for (int guard = 0; !done && guard < L + Wd + Hz + 4; guard += kAhead) {
 #pragma unroll
         for (int k = 0; k < kAhead; ++k) {
-            if (!inside_grid(ix, iy, iz)) {
+            const int c = code[k];
+            if (!(c & 4)) {
                 done = true;
                 break;
             }
             const float cur = View::decode(ring[k]);
-            ring[k] = inside_grid(ax, ay, az) ? vol.raw(ali) : typename View::Raw(0);
-            lead_step();
+            const bool in = inside_grid(ax, ay, az);
+            ring[k] = in ? vol.raw(ali) : typename View::Raw(0);
+            code[k] = (in ? 4 : 0) | lead_step();
             // the reference's four tests (:207-222) are mutually exclusive in prev
             const bool stop = prev < 0.f ? !(cur <= 0.f) : (isnan(prev) && cur < 0.f);
             if (stop) {
@@ -438,8 +447,8 @@ __device__ __forceinline__ void trace(const View& vol, float X, float Y, float D
                 break;
             }
             prev = cur;
-            bool bx, by, bz;
-            pick(tm, bx, by, bz);
+            const int axis = c & 3;
+            const bool bx = axis == 0, by = axis == 1, bz = axis == 2;
             const int ox = ix, oy = iy, oz = iz;
             XY = bx ? oy : XY;
             XZ = bx ? oz : XZ;
@@ -451,10 +460,6 @@ __device__ __forceinline__ void trace(const View& vol, float X, float Y, float D
             iy += by ? sy : 0;
             iz += bz ? sz : 0;
             li += bx ? dlx : (by ? dly : dlz);
-            const float nx = tm.x + td.x, ny = tm.y + td.y, nz = tm.z + td.z;
-            tm.x = bx ? nx : tm.x;
-            tm.y = by ? ny : tm.y;
-            tm.z = bz ? nz : tm.z;
         }
     }
     if (!(crossing < 0.f)) return;
