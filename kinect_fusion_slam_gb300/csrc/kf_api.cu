@@ -331,7 +331,7 @@ kf_status allocate(kf_handle* h)
     KF_TRY(dalloc(h, &h->d_pn, HW));
     KF_TRY(dalloc(h, &h->d_hit, HW));
     KF_TRY(dalloc(h, &h->d_pair, HW));
-    KF_TRY(dalloc(h, &h->d_tab, HW));
+    KF_TRY(dalloc(h, &h->d_tab, HW + depth_bound_tiles(h->cam.H, h->cam.W)));
     KF_TRY(dalloc(h, &h->d_state, 1));
     KF_TRY(dalloc(h, &h->d_partials, icp_scratch_floats(h->cam.H, h->cam.W)));
     KF_TRY(dalloc(h, &h->d_groups, (size_t)icp_groups(h->cam.H, h->cam.W)));

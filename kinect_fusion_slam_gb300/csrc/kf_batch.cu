@@ -75,6 +75,8 @@ void fill_table(kf_batch* b)
         d.dmin = h->cfg.min_depth;
         d.dmax = h->cfg.max_depth;
         d.band = 3.0f * h->cfg.sigma_r;
+        d.depth_eps = depth_band_eps(h->cam);
+        d.lam_max = ray_norm_max(h->cam);
         for (int sh = 0; sh < 3; ++sh) {
             d.tile_start[sh] = start[sh];
             start[sh] += raycast_tiles(h->cam.H, h->cam.W, sh);

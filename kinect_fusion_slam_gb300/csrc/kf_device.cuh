@@ -84,6 +84,8 @@ struct SceneDev {
     long long skip_from;
     float dmin, dmax, band;
     int tile_start[3];  // first ray-cast tile of this scene for tile shapes 8x4, 16x2, 4x8
+    float depth_eps;    // integration's depth-band cull margin (depth_band_eps)
+    float lam_max;      // ray_norm_max
 };
 
 // voxel-centre coordinate, kinfu_pipeline.cpp:53-55: x * voxel_distance + voxel_distance / 2

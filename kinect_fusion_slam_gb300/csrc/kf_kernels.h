@@ -43,9 +43,17 @@ void launch_icp_associate(const float4* vmap, const float4* nmap, const float4* 
                           float* partials, int* list, float* sums_out, int32_t* pair, cudaStream_t s);
 
 // per-pixel integration table + T^-1 and the in-front axis into st
+// the integration table (per pixel) and, after its H*W entries, the 8x8-tile depth
+// bounds: tab must hold H*W + depth_bound_tiles(H, W) entries
 void launch_integrate_prep(const float* depth, float2* tab, const Camera& cam, State* st, cudaStream_t s);
-// projective TSDF update (projective_tsdf.cu:5-140); skip_from = first z-fastest index
-// the reference's float guard never reaches
+int depth_bound_tiles(int H, int W);
+// relative margin of integration's depth-band cull for this camera
+float depth_band_eps(const Camera& cam);
+// largest |K^-1 (u, v, 1)| over the image (with a margin)
+float ray_norm_max(const Camera& cam);
+// projective TSDF update (projective_tsdf.cu:5-140) in 32x8x16 voxel boxes, skipping
+// boxes and column segments that provably hold no updated voxel; skip_from = first
+// z-fastest index the reference's float guard never reaches
 void launch_integrate_f32(float* tsdf, float* weight, const float2* tab, const State* st, const Grid& g,
                           const Camera& cam, long long skip_from, bool first, cudaStream_t s);
 void launch_integrate_f16(__half2* vol, const float2* tab, const State* st, const Grid& g, const Camera& cam,

@@ -105,39 +105,302 @@ __device__ __forceinline__ void integrate_prep_at(int i, const float* __restrict
     tab[i] = make_float2(D != 0 ? pd : qnan(), 1.f / mag);
 }
 
+// Per 8x8-pixel tile of the depth image: (min, max) of its nonzero |depth|, (+inf, -inf)
+// where it has none.  The table's distance entry is |D| times a factor within rounding
+// of 1 (the norm of D times the ray over the ray's norm), so these bound the entries
+// integration would read there.  Stored after the table's H*W entries.
+constexpr int kBoundTile = 8;
+
+__device__ __forceinline__ int bound_tiles_x(int W) { return (W + kBoundTile - 1) / kBoundTile; }
+
+// one warp per tile, two pixels per lane: the table entries of the tile's pixels and the
+// tile's depth bounds
+__device__ __forceinline__ void integrate_prep_tile(int tile, int lane, const float* __restrict__ depth,
+                                                    float2* __restrict__ tab, const Camera& cam, State* st)
+{
+    const int H = cam.H, W = cam.W;
+    const int ntx = bound_tiles_x(W);
+    const int x0 = (tile % ntx) * kBoundTile, y0 = (tile / ntx) * kBoundTile;
+    float lo = INFINITY, hi = -INFINITY;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const int x = x0 + (lane & 7), y = y0 + (lane >> 3) + 4 * h;
+        if (x < W && y < H) {
+            const int i = y * W + x;
+            integrate_prep_at(i, depth, tab, cam, st);
+            const float d = fabsf(depth[i]);
+            if (d != 0.f) {
+                lo = fminf(lo, d);
+                hi = fmaxf(hi, d);
+            }
+        }
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, off));
+        hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, off));
+    }
+    if (lane == 0) tab[H * W + tile] = make_float2(lo, hi);
+}
+
 __global__ void __launch_bounds__(256) integrate_prep_kernel(const float* __restrict__ depth, float2* __restrict__ tab,
                                                              Camera cam, State* st)
 {
     wait_for_producer();
-    integrate_prep_at(blockIdx.x * blockDim.x + threadIdx.x, depth, tab, cam, st);
+    const int tiles = bound_tiles_x(cam.W) * ((cam.H + kBoundTile - 1) / kBoundTile);
+    const int tile = blockIdx.x * 8 + (threadIdx.x >> 5);
+    if (tile < tiles) integrate_prep_tile(tile, threadIdx.x & 31, depth, tab, cam, st);
 }
 
 __global__ void __launch_bounds__(256) integrate_prep_batch_kernel(const SceneDev* __restrict__ scenes)
 {
     wait_for_producer();
     const SceneDev& d = scenes[blockIdx.y];
-    integrate_prep_at(blockIdx.x * blockDim.x + threadIdx.x, d.depth[0], d.tab, d.cam[0], d.st);
+    const Camera& cam = d.cam[0];
+    const int tiles = bound_tiles_x(cam.W) * ((cam.H + kBoundTile - 1) / kBoundTile);
+    for (int tile = blockIdx.x * 8 + (threadIdx.x >> 5); tile < tiles; tile += gridDim.x * 8)
+        integrate_prep_tile(tile, threadIdx.x & 31, d.depth[0], d.tab, cam, d.st);
 }
 
+// Integration proceeds in boxes of kIntTx x kIntTy voxel columns by zchunk voxels along
+// z: one block of kIntTx x kIntTy threads per box, one thread per column segment.  A box
+// is culled as a whole, then each surviving thread's segment, then each voxel.
 constexpr int kIntTx = 32, kIntTy = 8;
+
+// The frame's constants of integration beside the pose (which the kernels read from
+// State).
+struct IntegrateParams {
+    float fx, fy, cx, cy;
+    int H, W;
+    int zchunk;
+    long long skip_from;
+    float depth_eps;  // relative depth margin of the depth-band cull (depth_band_eps)
+    float lam_max;    // largest |K^-1 (u, v, 1)| over the image
+};
+
+__device__ __forceinline__ IntegrateParams scene_params(const SceneDev& d, int zchunk)
+{
+    const Camera& c = d.cam[0];
+    return IntegrateParams{c.K[0], c.K[4], c.K[2], c.K[5], c.H, c.W, zchunk, d.skip_from, d.depth_eps, d.lam_max};
+}
+
+// Bounds of what integration computes over a set of voxel centres.  Every quantity the
+// per-voxel tests use is affine in the centre (the in-front value, the camera-frame
+// coordinates) or, while the camera depth lz stays positive, a ratio of affine
+// functions (the projection q = (f l + c lz) / lz), so over a box of centres (or a
+// segment) their extremes are attained at its corners (ends): for a centre that is a
+// convex combination of corners, f l + c lz - q_k lz < 0 at every corner implies it for
+// the centre.  The magnitude sums bound the float rounding of each evaluation.
+struct Extent {
+    float front, fmag;     // largest in-front value; largest sum of its terms' magnitudes
+    float lz_lo, lz_hi;    // camera depth range
+    float qu_lo, qu_hi;    // projection range (meaningful while lz_lo > 0)
+    float qv_lo, qv_hi;
+    float lmag;            // largest magnitude sum of a camera-frame coordinate's terms
+};
+
+__device__ __forceinline__ Extent corner_extent(const float* ti, float tx, float ty, float tz, float ax, float ay,
+                                                float az, float vcx, float vcy, float vcz, const IntegrateParams& p)
+{
+    Extent e;
+    const float tdx = vcx - tx, tdy = vcy - ty, tdz = vcz - tz;
+    e.front = (ax * tdx + ay * tdy) + az * tdz;
+    e.fmag = fabsf(ax * tdx) + fabsf(ay * tdy) + fabsf(az * tdz);
+    const float lx = (ti[0] * vcx + ti[1] * vcy) + ti[2] * vcz + ti[3];
+    const float ly = (ti[4] * vcx + ti[5] * vcy) + ti[6] * vcz + ti[7];
+    const float lz = (ti[8] * vcx + ti[9] * vcy) + ti[10] * vcz + ti[11];
+    e.lz_lo = e.lz_hi = lz;
+    e.qu_lo = e.qu_hi = (p.fx * lx + p.cx * lz) / lz;
+    e.qv_lo = e.qv_hi = (p.fy * ly + p.cy * lz) / lz;
+    float m = 0.f;
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+        m = fmaxf(m, fabsf(ti[4 * r] * vcx) + fabsf(ti[4 * r + 1] * vcy) + fabsf(ti[4 * r + 2] * vcz) +
+                         fabsf(ti[4 * r + 3]));
+    e.lmag = m;
+    return e;
+}
+
+__device__ __forceinline__ void merge_extent(Extent& a, const Extent& b)
+{
+    a.front = fmaxf(a.front, b.front);
+    a.fmag = fmaxf(a.fmag, b.fmag);
+    a.lz_lo = fminf(a.lz_lo, b.lz_lo);
+    a.lz_hi = fmaxf(a.lz_hi, b.lz_hi);
+    a.qu_lo = fminf(a.qu_lo, b.qu_lo);
+    a.qu_hi = fmaxf(a.qu_hi, b.qu_hi);
+    a.qv_lo = fminf(a.qv_lo, b.qv_lo);
+    a.qv_hi = fmaxf(a.qv_hi, b.qv_hi);
+    a.lmag = fmaxf(a.lmag, b.lmag);
+}
+
+__device__ __forceinline__ Extent shfl_xor_extent(const Extent& e, int off)
+{
+    Extent o;
+    o.front = __shfl_xor_sync(0xffffffffu, e.front, off);
+    o.fmag = __shfl_xor_sync(0xffffffffu, e.fmag, off);
+    o.lz_lo = __shfl_xor_sync(0xffffffffu, e.lz_lo, off);
+    o.lz_hi = __shfl_xor_sync(0xffffffffu, e.lz_hi, off);
+    o.qu_lo = __shfl_xor_sync(0xffffffffu, e.qu_lo, off);
+    o.qu_hi = __shfl_xor_sync(0xffffffffu, e.qu_hi, off);
+    o.qv_lo = __shfl_xor_sync(0xffffffffu, e.qv_lo, off);
+    o.qv_hi = __shfl_xor_sync(0xffffffffu, e.qv_hi, off);
+    o.lmag = __shfl_xor_sync(0xffffffffu, e.lmag, off);
+    return o;
+}
+
+// Pixel footprint of an extent that survived the frustum test: the image rows and
+// columns (0-based) its centres can round to, as 8x8-tile ranges.
+struct Footprint {
+    int tx0, tx1, ty0, ty1;
+    float lz_lo, lz_hi;  // widened by the evaluation error
+};
+
+// 0: some centre may be updated and the footprint is not known (keep); 1: no centre can
+// be updated (cull); 2: the depth-band test over footprint fp decides.
+//
+// Margins.  A voxel's own evaluation and a corner's differ from the exact affine values
+// by a few roundings of their partial sums: err_l = 2^-20 lmag bounds both for the
+// camera coordinates (5 roundings of at most 2^-24 lmag each, twice), and
+// 1e-2 + 1e-5 fmag for the in-front value.  A voxel is kept by the projection test iff
+// its rounded q lies in [0.5, W + 0.5); a q bound moves by at most
+// (f + |c| + |q|) err_l / lz + 2^-20 |q| when the coordinates move by err_l, and one
+// more pixel is added on top.
+__device__ __forceinline__ int extent_cull(const Extent& e, const IntegrateParams& p, Footprint& fp)
+{
+    const float fm = 1e-2f + 1e-5f * e.fmag;
+    if (e.front < -fm) return 1;
+    const float err_l = e.lmag * 0x1p-20f;
+    const float lz_lo = e.lz_lo - err_l;
+    if (!(lz_lo > 50.f)) return 0;
+    const float qabs = fmaxf(fmaxf(fabsf(e.qu_lo), fabsf(e.qu_hi)), fmaxf(fabsf(e.qv_lo), fabsf(e.qv_hi)));
+    const float mq = 1.f + (fmaxf(p.fx, p.fy) + fmaxf(fabsf(p.cx), fabsf(p.cy)) + qabs) * err_l / lz_lo +
+                     qabs * 0x1p-20f;
+    if (e.qu_hi < 0.5f - mq || e.qu_lo >= (float)p.W + 0.5f + mq || e.qv_hi < 0.5f - mq ||
+        e.qv_lo >= (float)p.H + 0.5f + mq)
+        return 1;
+    // column u - 1 of u = round(q) for q in [qu_lo - mq, qu_hi + mq], clamped to the image
+    const float W1 = (float)(p.W - 1), H1 = (float)(p.H - 1);
+    const int c0 = (int)fminf(fmaxf(floorf(e.qu_lo - mq) - 1.f, 0.f), W1);
+    const int c1 = (int)fminf(fmaxf(floorf(e.qu_hi + mq), 0.f), W1);
+    const int r0 = (int)fminf(fmaxf(floorf(e.qv_lo - mq) - 1.f, 0.f), H1);
+    const int r1 = (int)fminf(fmaxf(floorf(e.qv_hi + mq), 0.f), H1);
+    fp.tx0 = c0 / kBoundTile;
+    fp.tx1 = c1 / kBoundTile;
+    fp.ty0 = r0 / kBoundTile;
+    fp.ty1 = r1 / kBoundTile;
+    fp.lz_lo = lz_lo;
+    fp.lz_hi = e.lz_hi + err_l;
+    return 2;
+}
+
+// Depth-band test.  A voxel is updated only if frk = D' - tm / m lies in [sdf_min,
+// sdf_max] (widened to contain 0), D' being the table's distance for its pixel and
+// tm / m the voxel's distance from the camera over the pixel ray's norm.  With the pixel
+// centre within half a pixel of the voxel's projection, tm / m is lz times a factor
+// within depth_eps of 1.  The table's entries are computed from the pose: D' is |D| to
+// within a relative eps_t plus an absolute 2^-19 |t| (rounding against the translation
+// t), and m to within eps_t.  With dmin, dmax the tile bounds of |D| over the footprint,
+// no voxel is updated if all of them are more than the band in front of every depth or
+// behind it, with another millimetre for the rounding of frk itself.
+__device__ __forceinline__ bool band_culled(const Footprint& fp, float dmin, float dmax, const IntegrateParams& p,
+                                            const Grid& g, const State* __restrict__ st)
+{
+    const float tmax = fmaxf(fmaxf(fabsf(st->T[3]), fabsf(st->T[7])), fabsf(st->T[11]));
+    const float eps_t = 0x1p-18f * (tmax + 4.f * p.lam_max + 1.f);
+    const float abs_t = 0x1p-19f * tmax + 1.f;
+    const float hi_band = fmaxf(g.sdf_max, 0.f), lo_band = fminf(g.sdf_min, 0.f);
+    const bool all_ahead = fp.lz_hi * (1.f + p.depth_eps) * (1.f + eps_t) + abs_t < dmin * (1.f - eps_t) - hi_band - abs_t;
+    const bool all_behind =
+        fp.lz_lo * (1.f - p.depth_eps) * (1.f - eps_t) - abs_t > dmax * (1.f + eps_t) - lo_band + abs_t;
+    return all_ahead || all_behind;
+}
+
+__device__ __forceinline__ void load_pose(const State* __restrict__ st, float* ti, float& tx, float& ty, float& tz,
+                                          float& ax, float& ay, float& az)
+{
+#pragma unroll
+    for (int k = 0; k < 12; ++k) ti[k] = st->Tinv[k];
+    tx = st->T[3];
+    ty = st->T[7];
+    tz = st->T[11];
+    ax = st->axis[0];
+    ay = st->axis[1];
+    az = st->axis[2];
+}
+
+// Box cull, run by one warp for its block's box of kIntTx x kIntTy columns x zchunk
+// voxels: lanes 0..7 (and their copies in each group of 8) evaluate the box's eight
+// corner centres, the warp merges them, and all lanes read the footprint's tile bounds.
+// False if no voxel of the box can be updated.
+__device__ __forceinline__ bool box_live(int bx, int by, int bz, int lane, const Grid& g,
+                                         const State* __restrict__ st, const float2* __restrict__ bounds,
+                                         const IntegrateParams& p)
+{
+    float ti[12], tx, ty, tz, ax, ay, az;
+    load_pose(st, ti, tx, ty, tz, ax, ay, az);
+    const int c = lane & 7;
+    const int ix = (c & 1) ? min(g.dx, bx * kIntTx + kIntTx) - 1 : bx * kIntTx;
+    const int iy = (c & 2) ? min(g.dy, by * kIntTy + kIntTy) - 1 : by * kIntTy;
+    const int iz = (c & 4) ? min(g.dz, bz * p.zchunk + p.zchunk) - 1 : bz * p.zchunk;
+    Extent e = corner_extent(ti, tx, ty, tz, ax, ay, az, centre(ix, g.sx, g.vd), centre(iy, g.sy, g.vd),
+                             centre(iz, g.sz, g.vd), p);
+#pragma unroll
+    for (int off = 1; off < 8; off <<= 1) merge_extent(e, shfl_xor_extent(e, off));
+    Footprint fp;
+    const int r = extent_cull(e, p, fp);  // the same in every lane
+    if (r != 2) return r == 0;
+    const int ntx = bound_tiles_x(p.W), w = fp.tx1 - fp.tx0 + 1;
+    const int n = w * (fp.ty1 - fp.ty0 + 1);
+    float dmin = INFINITY, dmax = -INFINITY;
+    for (int k = lane; k < n; k += 32) {
+        const float2 b = __ldg(bounds + (fp.ty0 + k / w) * ntx + fp.tx0 + k % w);
+        dmin = fminf(dmin, b.x);
+        dmax = fmaxf(dmax, b.y);
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        dmin = fminf(dmin, __shfl_xor_sync(0xffffffffu, dmin, off));
+        dmax = fmaxf(dmax, __shfl_xor_sync(0xffffffffu, dmax, off));
+    }
+    return !band_culled(fp, dmin, dmax, p, g, st);
+}
 
 template <class Vol, bool FIRST>
 __device__ __forceinline__ void integrate_at(const Vol& vol, const float2* __restrict__ tab,
-                                             const State* __restrict__ st, const Grid& g, float fx, float fy, float cx,
-                                             float cy, int H, int W, int zchunk, long long skip_from, int bx, int by,
-                                             int bz)
+                                             const State* __restrict__ st, const Grid& g, const IntegrateParams& p,
+                                             int bx, int by, int bz)
 {
     const int x = bx * kIntTx + threadIdx.x;
     const int y = by * kIntTy + threadIdx.y;
     if (x >= g.dx || y >= g.dy) return;
-    const int z0 = bz * zchunk;
-    const int z1 = min(z0 + zchunk, g.dz);
-    float ti[12];
-#pragma unroll
-    for (int k = 0; k < 12; ++k) ti[k] = st->Tinv[k];
-    const float tx = st->T[3], ty = st->T[7], tz = st->T[11];
-    const float ax = st->axis[0], ay = st->axis[1], az = st->axis[2];
+    const int z0 = bz * p.zchunk;
+    const int z1 = min(z0 + p.zchunk, g.dz);
+    const int H = p.H, W = p.W;
+    const float fx = p.fx, fy = p.fy, cx = p.cx, cy = p.cy;
+    float ti[12], tx, ty, tz, ax, ay, az;
+    load_pose(st, ti, tx, ty, tz, ax, ay, az);
     const float vcx = centre(x, g.sx, g.vd), vcy = centre(y, g.sy, g.vd);
+    {
+        // the same cull for this thread's segment of the column (its two end centres)
+        Extent e = corner_extent(ti, tx, ty, tz, ax, ay, az, vcx, vcy, centre(z0, g.sz, g.vd), p);
+        merge_extent(e, corner_extent(ti, tx, ty, tz, ax, ay, az, vcx, vcy, centre(z1 - 1, g.sz, g.vd), p));
+        Footprint fp;
+        const int r = extent_cull(e, p, fp);
+        if (r == 1) return;
+        if (r == 2 && (fp.tx1 - fp.tx0 + 1) * (fp.ty1 - fp.ty0 + 1) <= 16) {
+            const int ntx = bound_tiles_x(W);
+            const float2* bounds = tab + H * W;
+            float dmin = INFINITY, dmax = -INFINITY;
+            for (int ty_ = fp.ty0; ty_ <= fp.ty1; ++ty_)
+                for (int tx_ = fp.tx0; tx_ <= fp.tx1; ++tx_) {
+                    const float2 b = __ldg(bounds + ty_ * ntx + tx_);
+                    dmin = fminf(dmin, b.x);
+                    dmax = fmaxf(dmax, b.y);
+                }
+            if (band_culled(fp, dmin, dmax, p, g, st)) return;
+        }
+    }
     // the first two products of each row of T^-1 c and of the in-front dot product and
     // |c - t|^2 are the same along the column (left-to-right evaluation)
     const float a0 = ti[0] * vcx + ti[1] * vcy;
@@ -146,38 +409,10 @@ __device__ __forceinline__ void integrate_at(const Vol& vol, const float2* __res
     const float tdx = vcx - tx, tdy = vcy - ty;
     const float f0 = ax * tdx + ay * tdy;
     const float m0 = tdx * tdx + tdy * tdy;
-    {
-        // Chunk cull.  The chunk's voxels lie on a segment along z.  The in-front value
-        // front(z) = f0 + az (vcz - tz) and lz(z) are affine in the voxel centre vcz
-        // (monotone in z), and while lz > 50 mm on the whole segment the projection
-        // q(z) = (fx lx + cx lz) / lz is monotone too, so its values at the two ends bound
-        // every voxel's.  The margins (1e-2 mm + 1e-5 relative on front, 1 pixel on q)
-        // exceed the float error of any single voxel's evaluation by orders of magnitude,
-        // so a culled chunk holds no voxel the per-voxel tests below would accept.
-        float fr[2], lzv[2], qu[2], qv[2];
-#pragma unroll
-        for (int e = 0; e < 2; ++e) {
-            const float vcz = centre(e == 0 ? z0 : z1 - 1, g.sz, g.vd);
-            fr[e] = f0 + az * (vcz - tz);
-            const float lx = (a0 + ti[2] * vcz) + ti[3];
-            const float ly = (a1 + ti[6] * vcz) + ti[7];
-            lzv[e] = (a2 + ti[10] * vcz) + ti[11];
-            qu[e] = (fx * lx + cx * lzv[e]) / lzv[e];
-            qv[e] = (fy * ly + cy * lzv[e]) / lzv[e];
-        }
-        const float fm = 1e-2f + 1e-5f * (fabsf(f0) + fabsf(fr[0]) + fabsf(fr[1]));
-        bool cull = fr[0] < -fm && fr[1] < -fm;
-        if (!cull && lzv[0] > 50.f && lzv[1] > 50.f) {
-            const float lo = 0.5f - 1.f, hu = (float)W + 1.5f, hv = (float)H + 1.5f;
-            cull = (qu[0] < lo && qu[1] < lo) || (qu[0] > hu && qu[1] > hu) || (qv[0] < lo && qv[1] < lo) ||
-                   (qv[0] > hv && qv[1] > hv);
-        }
-        if (cull) return;
-    }
     const long long rbase = ((long long)x * g.dy + y) * g.dz;
     // the reference's guard compares the thread index with the voxel count in float, so
     // the last z-fastest indices are never integrated; only the last columns get there
-    const bool may_skip = rbase + z1 > skip_from;
+    const bool may_skip = rbase + z1 > p.skip_from;
     const int zstride = g.dx * g.dy;  // < 2^31 voxels (checked at kf_create)
     int lin = (z0 * g.dy + y) * g.dx + x;
     // a voxel projects to a pixel of the image iff q = px/pz lies in [0.5, W + 0.5) (and
@@ -187,7 +422,7 @@ __device__ __forceinline__ void integrate_at(const Vol& vol, const float2* __res
     const float ulo = 0.5f - 1e-3f, uhi = (float)W + 0.5f + 1e-3f * (float)W;
     const float vlo = 0.5f - 1e-3f, vhi = (float)H + 0.5f + 1e-3f * (float)H;
     for (int z = z0; z < z1; ++z, lin += zstride) {
-        if (may_skip && rbase + z >= skip_from) continue;
+        if (may_skip && rbase + z >= p.skip_from) continue;
         const float vcz = centre(z, g.sz, g.vd);
         // the reference's tests are independent rejections (all must pass), so the
         // cheapest runs first: the in-front test (:57-73) needs no projection
@@ -229,24 +464,38 @@ __device__ __forceinline__ void integrate_at(const Vol& vol, const float2* __res
     }
 }
 
+// One block per box.  Warp 0 decides whether the box can hold an updated voxel; a dead
+// box's other warps do nothing but wait for that decision.
 template <class Vol, bool FIRST>
-__global__ void __launch_bounds__(kIntTx* kIntTy) integrate_kernel(Vol vol, const float2* __restrict__ tab,
-                                                                   const State* __restrict__ st, Grid g, float fx,
-                                                                   float fy, float cx, float cy, int H, int W,
-                                                                   int zchunk, long long skip_from)
+__device__ __forceinline__ void integrate_box(const Vol& vol, const float2* __restrict__ tab,
+                                              const State* __restrict__ st, const Grid& g, const IntegrateParams& p,
+                                              int bx, int by, int bz)
+{
+    __shared__ int s_live;
+    if (threadIdx.y == 0) {
+        const bool live = box_live(bx, by, bz, threadIdx.x, g, st, tab + p.H * p.W, p);
+        if (threadIdx.x == 0) s_live = live;
+    }
+    __syncthreads();
+    if (s_live) integrate_at<Vol, FIRST>(vol, tab, st, g, p, bx, by, bz);
+}
+
+template <class Vol, bool FIRST>
+__global__ void __launch_bounds__(kIntTx* kIntTy, 5) integrate_kernel(Vol vol, const float2* __restrict__ tab,
+                                                                   const State* __restrict__ st, Grid g,
+                                                                   IntegrateParams p)
 {
     wait_for_producer();
-    integrate_at<Vol, FIRST>(vol, tab, st, g, fx, fy, cx, cy, H, W, zchunk, skip_from, blockIdx.x, blockIdx.y,
-                             blockIdx.z);
+    integrate_box<Vol, FIRST>(vol, tab, st, g, p, blockIdx.x, blockIdx.y, blockIdx.z);
 }
 
 __device__ __forceinline__ VolF32 scene_volume(const SceneDev& d, VolF32*) { return VolF32{d.tsdf, d.weight}; }
 __device__ __forceinline__ VolF16 scene_volume(const SceneDev& d, VolF16*) { return VolF16{d.vol16}; }
 
-// every scene's integration: blockIdx.y picks the scene, blockIdx.x its (x, y, z-chunk)
-// tile; scenes with fewer tiles than the largest return early
+// every scene's integration: blockIdx.y picks the scene, blockIdx.x its box; scenes with
+// fewer boxes than the largest return early
 template <class Vol, bool FIRST>
-__global__ void __launch_bounds__(kIntTx* kIntTy) integrate_batch_kernel(const SceneDev* __restrict__ scenes, int zchunk)
+__global__ void __launch_bounds__(kIntTx* kIntTy, 5) integrate_batch_kernel(const SceneDev* __restrict__ scenes, int zchunk)
 {
     wait_for_producer();
     const SceneDev& d = scenes[blockIdx.y];
@@ -254,10 +503,9 @@ __global__ void __launch_bounds__(kIntTx* kIntTy) integrate_batch_kernel(const S
     const int nbx = (g.dx + kIntTx - 1) / kIntTx, nby = (g.dy + kIntTy - 1) / kIntTy, nbz = (g.dz + zchunk - 1) / zchunk;
     const int t = blockIdx.x;
     if (t >= nbx * nby * nbz) return;
-    const Camera& cam = d.cam[0];
     const Vol vol = scene_volume(d, (Vol*)nullptr);
-    integrate_at<Vol, FIRST>(vol, d.tab, d.st, g, cam.K[0], cam.K[4], cam.K[2], cam.K[5], cam.H, cam.W, zchunk,
-                             d.skip_from, t % nbx, (t / nbx) % nby, t / (nbx * nby));
+    integrate_box<Vol, FIRST>(vol, d.tab, d.st, g, scene_params(d, zchunk), t % nbx, (t / nbx) % nby,
+                              t / (nbx * nby));
 }
 
 // Ray_Box_Intersection, voxel_traversal.cu:4-73
@@ -632,26 +880,63 @@ int raycast_blocks()
 
 void launch_integrate_prep(const float* depth, float2* tab, const Camera& cam, State* st, cudaStream_t s)
 {
-    const int n = cam.H * cam.W;
-    launch_pdl(integrate_prep_kernel, dim3((n + 255) / 256), dim3(256), 0, s, depth, tab, cam, st);
+    launch_pdl(integrate_prep_kernel, dim3((depth_bound_tiles(cam.H, cam.W) + 7) / 8), dim3(256), 0, s, depth, tab,
+               cam, st);
+}
+
+int depth_bound_tiles(int H, int W)
+{
+    return ((W + kBoundTile - 1) / kBoundTile) * ((H + kBoundTile - 1) / kBoundTile);
+}
+
+float depth_band_eps(const Camera& cam)
+{
+    // |tm / |R lambda| - lz| / lz <= 2 |a| dx + dx^2 + 2 |b| dy + dy^2 with dx = 1/(2 fx),
+    // dy = 1/(2 fy) and |a|, |b| the largest |x/z|, |y/z| of a voxel projecting into the
+    // image; doubled, plus 1e-4 for float rounding
+    const float fx = cam.K[0], fy = cam.K[4], cx = cam.K[2], cy = cam.K[5];
+    const float a = (fmaxf(cx, (float)cam.W + 1.f - cx) + 1.f) / fx, b = (fmaxf(cy, (float)cam.H + 1.f - cy) + 1.f) / fy;
+    const float dx = 0.5f / fx, dy = 0.5f / fy;
+    return 2.f * (2.f * a * dx + dx * dx + 2.f * b * dy + dy * dy) + 1e-4f;
+}
+
+float ray_norm_max(const Camera& cam)
+{
+    // |K^-1 (u, v, 1)| is convex in (u, v): its largest value is at a corner pixel
+    double m = 0.0;
+    for (int cu = 0; cu < 2; ++cu)
+        for (int cv = 0; cv < 2; ++cv) {
+            const double u = cu ? cam.W : 1, v = cv ? cam.H : 1;
+            double n = 0.0;
+            for (int r = 0; r < 3; ++r) {
+                const double c = (double)cam.Ki[3 * r] * u + (double)cam.Ki[3 * r + 1] * v + (double)cam.Ki[3 * r + 2];
+                n += c * c;
+            }
+            m = std::max(m, std::sqrt(n));
+        }
+    return (float)(m * 1.01 + 1e-3);
 }
 
 namespace {
 constexpr int kZChunk = 16;
 
+IntegrateParams host_params(const Camera& cam, int zchunk, long long skip_from)
+{
+    return IntegrateParams{cam.K[0], cam.K[4], cam.K[2], cam.K[5], cam.H, cam.W, zchunk, skip_from,
+                           depth_band_eps(cam), ray_norm_max(cam)};
+}
+
 template <class Vol>
 void integrate_launch(Vol vol, const float2* tab, const State* st, const Grid& g, const Camera& cam,
                       long long skip_from, bool first, cudaStream_t s)
 {
-    dim3 block(kIntTx, kIntTy);
-    dim3 grid((g.dx + kIntTx - 1) / kIntTx, (g.dy + kIntTy - 1) / kIntTy, (g.dz + kZChunk - 1) / kZChunk);
-    const float fx = cam.K[0], fy = cam.K[4], cx = cam.K[2], cy = cam.K[5];
+    const IntegrateParams p = host_params(cam, kZChunk, skip_from);
+    const dim3 block(kIntTx, kIntTy);
+    const dim3 grid((g.dx + kIntTx - 1) / kIntTx, (g.dy + kIntTy - 1) / kIntTy, (g.dz + kZChunk - 1) / kZChunk);
     if (first)
-        launch_pdl(integrate_kernel<Vol, true>, grid, block, 0, s, vol, tab, st, g, fx, fy, cx, cy, cam.H, cam.W,
-                   kZChunk, skip_from);
+        launch_pdl(integrate_kernel<Vol, true>, grid, block, 0, s, vol, tab, st, g, p);
     else
-        launch_pdl(integrate_kernel<Vol, false>, grid, block, 0, s, vol, tab, st, g, fx, fy, cx, cy, cam.H, cam.W,
-                   kZChunk, skip_from);
+        launch_pdl(integrate_kernel<Vol, false>, grid, block, 0, s, vol, tab, st, g, p);
 }
 }  // namespace
 
@@ -684,7 +969,7 @@ void launch_raycast_f16(const __half2* vol, const float* depth, float4* pv, floa
 void launch_integrate_batch(const SceneDev* scenes, int n_scenes, int max_pixels, int max_tiles, int zchunk, bool f16,
                             bool first, cudaStream_t s)
 {
-    launch_pdl(integrate_prep_batch_kernel, dim3((max_pixels + 255) / 256, n_scenes), dim3(256), 0, s, scenes);
+    launch_pdl(integrate_prep_batch_kernel, dim3((max_pixels / 64 + 7) / 8 + 1, n_scenes), dim3(256), 0, s, scenes);
     const dim3 grid(max_tiles, n_scenes), block(kIntTx, kIntTy);
     if (f16) {
         if (first)

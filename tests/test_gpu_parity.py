@@ -6,6 +6,8 @@ integrated voxels, ray-cast hit voxel indices, ICP correspondence pairings; floa
 within TSDF |d| <= 1e-6, points <= 1e-5 m (1e-2 mm), normals <= 1e-5, pose
 <= 1e-5 rad / 1e-5 m.
 """
+import dataclasses
+
 import numpy as np
 import pytest
 
@@ -69,6 +71,62 @@ def test_integration(oracle, small_seq, frame_pair):
     for n, k in enumerate(frame_pair):
         T = seq.poses[k].astype(np.float32)
         depth = oracle.depth_ingest(depths[k])
+        h.set_pose(T)
+        h.set_depth_f32(depth)
+        h.projective_tsdf(first=(n == 0))
+        oracle.integrate(gs, depth, K, Ki, T, oracle.inv4(T), to, wo, first=(n == 0))
+        tg, wg = h.volume()
+        assert_volume_parity(tg, wg, to, wo)
+    assert np.count_nonzero(~np.isnan(wo)) > 1000
+
+
+def _rot(yaw, pitch, roll):
+    cy, sy, cp, sp, cr, sr = np.cos(yaw), np.sin(yaw), np.cos(pitch), np.sin(pitch), np.cos(roll), np.sin(roll)
+    Rz = np.array([[cr, -sr, 0], [sr, cr, 0], [0, 0, 1]])
+    Ry = np.array([[cy, 0, sy], [0, 1, 0], [-sy, 0, cy]])
+    Rx = np.array([[1, 0, 0], [0, cp, -sp], [0, sp, cp]])
+    return Ry @ Rx @ Rz
+
+
+@pytest.mark.parametrize("offset_vox", [0, 2500])
+def test_integration_cull_exact(oracle, small_seq, offset_vox):
+    """Integration skips voxel boxes and column segments that provably hold no updated
+    voxel (behind the camera, outside the image, or beyond the truncation band of every
+    depth their pixels can read).  Hard cases for those proofs, bit for bit against the
+    oracle: oblique camera poses inside the grid, depths from 0.1 to 6 m with holes,
+    negative and isolated near samples, and the whole scene moved 50 m from the origin
+    (larger rounding against the translation)."""
+    seq, _ = small_seq
+    g = seq.cfg.grid
+    cam = seq.cfg.camera
+    off = float(offset_vox) * g.voxel_size
+    start = tuple(int(v) + offset_vox for v in g.start)
+    h = kf.Handle(kf.make_config(height=cam.height, width=cam.width, dims=g.dims, grid_start=start,
+                                 voxel_size=g.voxel_size))
+    K = seq.K
+    h.set_intrinsics(K[0, 0], K[1, 1], K[0, 2], K[1, 2])
+    gs = dataclasses.replace(grid_spec(g), start=start)
+    Ki = oracle.inv3(K)
+    rng = np.random.default_rng(5 + offset_vox)
+    H, W = cam.height, cam.width
+    to = np.full(gs.nvox, np.nan, np.float32)
+    wo = np.full(gs.nvox, np.nan, np.float32)
+    poses = [(0.3, 0.2, 0.0, (200.0, -150.0, -300.0)), (-0.5, -0.25, 0.3, (-400.0, 300.0, 100.0)),
+             (1.2, 0.1, -0.2, (0.0, 0.0, 500.0))]
+    for n, (yaw, pitch, roll, t) in enumerate(poses):
+        T = np.eye(4)
+        T[:3, :3] = _rot(yaw, pitch, roll)
+        T[:3, 3] = np.asarray(t) + off
+        T = T.astype(np.float32)
+        # smooth surface plus steps, holes and outliers
+        yy, xx = np.mgrid[0:H, 0:W]
+        depth = 1500.0 + 900.0 * np.sin(xx / 17.0) * np.cos(yy / 11.0) + 2000.0 * (xx > W // 2)
+        depth = depth.astype(np.float32)
+        depth[rng.random((H, W)) < 0.2] = 0.0
+        depth[rng.random((H, W)) < 0.01] = 100.0
+        depth[rng.random((H, W)) < 0.01] = 6000.0
+        depth[rng.random((H, W)) < 0.005] *= -1.0
+        depth[: H // 4, : W // 4] = 0.0
         h.set_pose(T)
         h.set_depth_f32(depth)
         h.projective_tsdf(first=(n == 0))
