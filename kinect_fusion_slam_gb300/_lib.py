@@ -139,6 +139,7 @@ SIGNATURES = {
     "kf_batch_autotune": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
     "kf_batch_set_tuning": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
     "kf_selftest_solve": (C.c_int, [C.c_ulonglong, C.c_int, C.c_int, C.POINTER(C.c_ulonglong)]),
+    "kf_selftest_solve6": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
     "kf_icp_associate_noalloc": (C.c_int, [C.c_int, C.c_int, _f32p, _f32p, _f32p, _vp, _vp, _vp, _vp, C.c_float,
                                            C.c_float, _vp, _vp, _vp]),
 }

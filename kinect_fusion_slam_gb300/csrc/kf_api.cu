@@ -176,7 +176,7 @@ void enq_icp(kf_handle* h)
     for (int l = L - 1; l >= 0; --l)
         for (int it = 0; it < h->cfg.icp_iterations[l]; ++it)
             launch_icp_iteration(h->d_vmap_l[l], h->d_nmap_l[l], h->d_pv_l[l], h->d_pn_l[l], h->lcam[l], h->icp,
-                                 h->d_state, h->d_partials, h->d_groups, h->stream);
+                                 h->d_state, h->d_partials, h->d_groups, h->d_fixacc, h->stream);
 }
 
 void enq_integrate(kf_handle* h, bool first)
@@ -334,6 +334,8 @@ kf_status allocate(kf_handle* h)
     KF_TRY(dalloc(h, &h->d_tab, HW + depth_bound_tiles(h->cam.H, h->cam.W)));
     KF_TRY(dalloc(h, &h->d_state, 1));
     KF_TRY(dalloc(h, &h->d_partials, icp_scratch_floats(h->cam.H, h->cam.W)));
+    KF_TRY(dalloc(h, &h->d_fixacc, icp_fixacc_words()));
+    KF_CUDA(h, cudaMemsetAsync(h->d_fixacc, 0, icp_fixacc_words() * sizeof(long long), h->stream));
     KF_TRY(dalloc(h, &h->d_groups, (size_t)icp_groups(h->cam.H, h->cam.W)));
     KF_TRY(dalloc(h, &h->d_tiles, 2));
     KF_CUDA(h, cudaMemset(h->d_tiles, 0, 2 * sizeof(unsigned)));
@@ -405,6 +407,7 @@ void free_all(kf_handle* h)
     destroy_graphs(h);
     void* dev[] = {h->d_raw, h->d_depth, h->d_depth_tmp, h->d_vmap, h->d_nmap, h->d_pv, h->d_pn, h->d_hit,
                    h->d_pair, h->d_tab, h->d_tsdf, h->d_weight, h->d_vol16, h->d_state, h->d_partials, h->d_groups,
+                   h->d_fixacc,
                    h->d_tiles, h->d_mats,
                    h->d_spatial};
     for (void* p : dev)
@@ -1102,8 +1105,8 @@ kf_status kf_icp_associate(kf_handle* h, const float F[16], const float T[16], i
     std::memcpy(mats + 16, T, sizeof(float) * 16);
     KF_CUDA(h, cudaMemcpyAsync(h->d_mats, mats, sizeof(mats), cudaMemcpyHostToDevice, h->stream));
     launch_icp_associate(h->d_vmap, h->d_nmap, h->d_pv, h->d_pn, h->cam, h->icp, h->d_mats, h->d_mats + 16,
-                         h->d_state, h->d_partials, h->d_groups, h->d_mats + 32, pair ? h->d_pair : nullptr,
-                         h->stream);
+                         h->d_state, h->d_partials, h->d_groups, h->d_fixacc, h->d_mats + 32,
+                         pair ? h->d_pair : nullptr, h->stream);
     KF_CHECK_LAUNCH(h);
     float sums[kIcpVals];
     KF_CUDA(h, cudaMemcpyAsync(sums, h->d_mats + 32, sizeof(sums), cudaMemcpyDeviceToHost, h->stream));

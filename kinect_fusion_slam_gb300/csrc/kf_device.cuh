@@ -37,9 +37,6 @@ struct IcpParams {
 
 // Per-handle device state, updated by the kernels so that a whole frame runs without
 // host round trips.
-// blocks of the precision form's ICP pass are reduced in at most this many slabs
-constexpr int kMaxSlabs = 64;
-
 struct State {
     float T[16];          // extrinsic_matrix: camera-to-world pose
     int error;            // set by a kernel whose bounded wait gave up (read with T)
@@ -50,12 +47,12 @@ struct State {
     float c_flip;         // ray-cast normal flip threshold (voxel_traversal.cu:361-369)
     double Td[16];        // FP64 pose (precise solve mode)
     unsigned ticket;      // last-block election counter of the ICP reduction
-    unsigned slab_ticket[kMaxSlabs];  // per-slab election counters of the precision form's reduction
     int iter;             // ICP iterations done in the current frame
     int32_t ncorr[kMaxIcpIters];
     int32_t chol_ok[kMaxIcpIters];
     float Tlog[kMaxIcpIters][16];  // pose after each iteration
     float sums[kIcpVals];  // sums of the most recent ICP iteration
+    unsigned fix_bad;      // precision form: sums whose block values could not be accumulated
 };
 
 // One scene of a batch (the batching form): the device buffers and parameters its

@@ -36,6 +36,7 @@ struct kf_handle {
     int32_t* d_hit = nullptr;
     int32_t* d_pair = nullptr;
     float2* d_tab = nullptr;
+    long long* d_fixacc = nullptr;  // the precision form's ICP accumulators (icp_fixacc_words)
     float* d_tsdf = nullptr;
     float* d_weight = nullptr;
     __half2* d_vol16 = nullptr;

@@ -252,56 +252,51 @@ __device__ void finish_iteration_warp(State* st, const IcpParams& prm, const flo
     }
 }
 
-// The precision form's update by one warp: the compensated sums (hi + lo) as FP64, the
-// FP64 Cholesky solve, and the SE(3) composition Inc * T applied to the FP64 pose (the
-// only FP64 steps); the float pose and F follow from it.
-__device__ void finish_precise_warp(State* st, const IcpParams& prm, const float* hi, const float* lo)
+// The precision form's update by one warp: the sums as FP64 (lane k < kIcpVals holds
+// sum k: b, then A's upper triangle by rows, then the correspondence count), the FP64
+// solve (warp_gj6_f64), and the SE(3) composition Inc * T applied to the FP64 pose (the
+// only FP64 steps); the float pose and F follow from it.  The previous pose is loaded
+// first so that its latency hides behind the solve.
+__device__ void finish_precise_warp(State* st, const IcpParams& prm, double val)
 {
-    __shared__ double A[36], x[6], r[6], inc[16], Tn[16];
     __shared__ float Tf[16], Tp[16];
-    __shared__ int fail;
     const int lane = threadIdx.x & 31;
     const int it = st->iter;
-    if (lane < 16) {
-        Tp[lane] = st->Tprev_inv[lane];
-        Tn[lane] = st->Td[lane];
+    const float tp = lane < 16 ? st->Tprev_inv[lane] : 0.f;
+    const double td = lane < 16 ? st->Td[lane] : 0.0;
+    if (lane < kIcpVals) st->sums[lane] = (float)val;
+    // lane c < 6: column c of A; lane 6: b
+    double col[6], b[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+        const int src = lane < 6 ? tri(min(i, lane), max(i, lane)) : i;
+        col[i] = __shfl_sync(0xffffffffu, val, src);
+        b[i] = col[i];
     }
-    // one sum per lane: b (lanes 0..5) or an entry of A's lower triangle (lanes 6..26)
-    if (lane < kIcpVals - 1) {
-        const double val = (double)hi[lane] + (double)lo[lane];
-        if (lane < 6) {
-            x[lane] = val;
-        } else {
-            int r = 0;
-            while (r < 5 && lane >= tri(r + 1, r + 1)) ++r;
-            const int c = r + (lane - tri(r, r));  // sums index tri(r, c), c >= r
-            A[c * 6 + r] = val;
-        }
-    }
-    if (lane < kIcpVals) st->sums[lane] = hi[lane] + lo[lane];
-    __syncwarp();
-    const bool ok = warp_chol6_f64(A, x, r, &fail);
-    if (lane == 0) {
-        if (!ok)  // the reference applies b as it stands, or the identity in that fail mode
-            for (int i = 0; i < 6; ++i) x[i] = prm.fail_mode == 1 ? 0.0 : (double)hi[i] + (double)lo[i];
-        const double e[16] = {1.0, x[2], -x[1], x[3], -x[2], 1.0, x[0], x[4],
-                              x[1], -x[0], 1.0, x[5], 0.0, 0.0, 0.0, 1.0};
-        for (int k = 0; k < 16; ++k) inc[k] = e[k];
-    }
-    __syncwarp();
-    double tn = 0.0;
-    if (lane < 16) {
-        const int rr = lane >> 2, c = lane & 3;
-        tn = inc[rr * 4] * Tn[c];
-        tn = fma(inc[rr * 4 + 1], Tn[4 + c], tn);
-        tn = fma(inc[rr * 4 + 2], Tn[8 + c], tn);
-        tn = fma(inc[rr * 4 + 3], Tn[12 + c], tn);
-    }
-    __syncwarp();
+    const bool ok = warp_gj6_f64(col);
+    const double count = __shfl_sync(0xffffffffu, val, kIcpVals - 1);
+    // the increment (omega, t) in every lane; where A is not positive definite the
+    // reference applies b as it stands, or the identity in that fail mode
+    double x[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) x[i] = __shfl_sync(0xffffffffu, ok ? col[i] : (prm.fail_mode == 1 ? 0.0 : b[i]), 6);
+    // row rr of Inc = [[1, w2, -w1, t0], [-w2, 1, w0, t1], [w1, -w0, 1, t2], [0, 0, 0, 1]]
+    const int rr = (lane >> 2) & 3, c = lane & 3;
+    const double i0 = rr == 0 ? 1.0 : rr == 1 ? -x[2] : rr == 2 ? x[1] : 0.0;
+    const double i1 = rr == 0 ? x[2] : rr == 1 ? 1.0 : rr == 2 ? -x[0] : 0.0;
+    const double i2 = rr == 0 ? -x[1] : rr == 1 ? x[0] : rr == 2 ? 1.0 : 0.0;
+    const double i3 = rr == 3 ? 1.0 : x[3 + rr];
+    const double t0 = __shfl_sync(0xffffffffu, td, c), t1 = __shfl_sync(0xffffffffu, td, 4 + c);
+    const double t2 = __shfl_sync(0xffffffffu, td, 8 + c), t3 = __shfl_sync(0xffffffffu, td, 12 + c);
+    double tn = i0 * t0;
+    tn = fma(i1, t1, tn);
+    tn = fma(i2, t2, tn);
+    tn = fma(i3, t3, tn);
     if (lane < 16) {
         st->Td[lane] = tn;
         Tf[lane] = (float)tn;
-        st->T[lane] = Tf[lane];
+        Tp[lane] = tp;
+        st->T[lane] = (float)tn;
     }
     __syncwarp();
     if (lane < 16) {
@@ -311,7 +306,7 @@ __device__ void finish_precise_warp(State* st, const IcpParams& prm, const float
     }
     if (lane == 0) {
         if (it < kMaxIcpIters) {
-            st->ncorr[it] = (int32_t)(hi[kIcpVals - 1] + lo[kIcpVals - 1]);
+            st->ncorr[it] = (int32_t)count;
             st->chol_ok[it] = ok ? 1 : 0;
         }
         st->iter = it + 1;
@@ -385,7 +380,8 @@ __global__ void __launch_bounds__(kIcpBlock) icp_kernel(const float4* __restrict
         return;
     }
     if (PRECISE) {
-        finish_precise_warp(st, prm, red_hi, red_lo);
+        const int k = threadIdx.x;
+        finish_precise_warp(st, prm, k < kIcpVals ? (double)red_hi[k] + (double)red_lo[k] : 0.0);
     } else {
         __shared__ float sT0[16], sTp[16];
         if (threadIdx.x < 16) {
@@ -674,73 +670,176 @@ __device__ __forceinline__ void solve_body(const float* __restrict__ partials, i
 
 // The precision form in one pass per iteration.  One warp per 64-pixel group forms the
 // group's 28 sums (as in the group pass); the block combines its groups with
-// compensated (TwoSum) FP32 and writes one hi/lo partial.  The blocks are then reduced
-// in two levels: the last block of each slab of consecutive blocks (a ticket per slab)
-// adds the slab's partials, and the last slab to finish adds the slab partials and
-// solves in FP64 (finish_precise_warp, MODE 0) or writes hi + lo (MODE 1).  A level
-// issues all its loads before adding, so its latency is about one trip to L2.
-// Summation order is free here: the precision form is held to the FP64 oracle, not to
-// the reference's bits.
-constexpr int kSlabRows = 32;
+// compensated (TwoSum) FP32 into a hi/lo pair per sum, and adds both to an exact
+// fixed-point accumulator: each value times 2^48, truncated toward zero, as a 128-bit
+// two's-complement integer whose four 32-bit digits go to four 64-bit accumulators by
+// atomic addition (integer addition commutes, so the result does not depend on the
+// order the blocks arrive in).  The last block to finish (a ticket) reads and clears
+// the accumulators, carries the digits into one integer per sum, converts it to FP64
+// and solves (finish_precise_warp, MODE 0) or writes the float sums (MODE 1).  Nothing
+// waits for a second pass over the partials.  Every block value below 2^79 in magnitude
+// is held exactly (to 2^-48), and the digit accumulators stay below 2^63 for fewer than
+// 2^31 blocks, so their sum is exact; a non-finite or larger block value marks its sum
+// NaN, as the float sum would have gone infinite or NaN.  The accumulators of a sum are
+// spread over kFixReplicas copies (block b adds to copy b % kFixReplicas), one 128-byte
+// line per digit and copy, so that few atomic additions queue on any one line.
+namespace fix {
 
-// Adds nrows rows of [hi(28) | lo(28)] with compensation into red_hi/red_lo (shared).
-// Four threads per column take every fourth row; all threads of the block call.
-__device__ __forceinline__ void reduce_rows(const float* rows, int nrows, float* red_hi, float* red_lo)
+// f * 2^48 truncated toward zero as a 128-bit two's-complement integer (hi, lo); false
+// for a non-finite f or |f| >= 2^79
+__device__ __forceinline__ bool to_fixed(float f, unsigned long long& hi, unsigned long long& lo)
 {
-    constexpr int kCols = 2 * kIcpVals;
-    constexpr int kLanes = (kExactWarps * 32) / kCols;
-    __shared__ float ph[kLanes][kIcpVals], pc[kLanes][kIcpVals], pl[kLanes][kIcpVals];
-    const int t = threadIdx.x;
-    if (t < kLanes * kCols) {
-        const int col = t % kCols, r0 = t / kCols;
-        float h = 0.f, l = 0.f;
-        for (int base = r0; base < nrows; base += kLanes * 8) {
-            float v[8];
+    const unsigned u = __float_as_uint(f);
+    const int e = (int)((u >> 23) & 0xffu);
+    hi = lo = 0ull;
+    if (e == 0xff || e > 205) return false;
+    const unsigned long long m = (u & 0x7fffffu) | (e ? 0x800000u : 0u);
+    const int sh = (e ? e : 1) - 102;  // |f| * 2^48 = m * 2^sh, m < 2^24, sh <= 103
+    if (sh >= 64) {
+        hi = m << (sh - 64);
+    } else if (sh > 40) {
+        hi = m >> (64 - sh);
+        lo = m << sh;
+    } else if (sh >= 0) {
+        lo = m << sh;
+    } else if (sh > -64) {
+        lo = m >> (-sh);
+    }
+    if (u >> 31) {
+        lo = ~lo + 1ull;
+        hi = ~hi + (lo == 0ull ? 1ull : 0ull);
+    }
+    return true;
+}
+
+constexpr int kFixReplicas = 16;
+
+// the accumulator of digit d of sum k in copy r
+__device__ __forceinline__ unsigned long long* digit(long long* acc, int k, int d, int r)
+{
+    return reinterpret_cast<unsigned long long*>(acc) + ((size_t)((k * 4 + d) * kFixReplicas + r) * 16);
+}
+
+// adds hi + lo (a compensated pair) to sum k's accumulator (replica r); flags sum k if
+// either part cannot be represented
+__device__ __forceinline__ void accumulate(long long* acc, unsigned* bad, int k, int r, float h, float l)
+{
+    unsigned long long h1, l1, h2, l2;
+    const bool ok = to_fixed(h, h1, l1) & to_fixed(l, h2, l2);
+    if (!ok) {
+        atomicOr(bad, 1u << k);
+        return;
+    }
+    const unsigned long long lo = l1 + l2;
+    const unsigned long long hi = h1 + h2 + (lo < l1 ? 1ull : 0ull);
+    atomicAdd(digit(acc, k, 0, r), lo & 0xffffffffull);
+    atomicAdd(digit(acc, k, 1, r), lo >> 32);
+    atomicAdd(digit(acc, k, 2, r), hi & 0xffffffffull);
+    atomicAdd(digit(acc, k, 3, r), (unsigned long long)((long long)hi >> 32));  // the signed top digit
+}
+
+// The last block's read-out, all threads of the block: each digit's replicas are read
+// (every load issued before any is used), added, and cleared; digits[k * 4 + d] (shared)
+// receives digit d of sum k.
+__device__ __forceinline__ void gather_digits(long long* acc, long long* digits)
+{
+    static_assert(kIcpVals * 4 * 2 <= kExactWarps * 32 && kFixReplicas % 2 == 0, "two threads per digit");
+    const int t = threadIdx.x, D = t >> 1, half = t & 1;
+    constexpr int kPer = kFixReplicas / 2;
+    long long v = 0;
+    if (D < kIcpVals * 4) {
+        unsigned long long* w[kPer];
+        unsigned long long x[kPer];
 #pragma unroll
-            for (int u = 0; u < 8; ++u) {
-                const int r = base + u * kLanes;
-                v[u] = r < nrows ? __ldcg(rows + (size_t)r * kCols + col) : 0.f;
-            }
-#pragma unroll
-            for (int u = 0; u < 8; ++u) {
-                float sum, e;
-                two_sum(h, v[u], sum, e);
-                h = sum;
-                l += e;
-            }
+        for (int i = 0; i < kPer; ++i) {
+            w[i] = digit(acc, D >> 2, D & 3, half * kPer + i);
+            x[i] = __ldcg(w[i]);
         }
-        if (col < kIcpVals) {
-            ph[r0][col] = h;
-            pc[r0][col] = l;
+#pragma unroll
+        for (int i = 0; i < kPer; ++i) {
+            v += (long long)x[i];
+            __stcg(w[i], 0ull);
+        }
+    }
+    v += __shfl_xor_sync(0xffffffffu, v, 1);
+    if (D < kIcpVals * 4 && half == 0) digits[D] = v;
+    __syncthreads();
+}
+
+// sum k from its carried digits (NaN if flagged)
+__device__ __forceinline__ double take(const long long* digits, int k, bool flagged)
+{
+    const long long d0 = digits[k * 4 + 0], d1 = digits[k * 4 + 1];
+    const long long d2 = digits[k * 4 + 2], d3 = digits[k * 4 + 3];
+    if (flagged) return __longlong_as_double(0x7ff8000000000000ll);
+    // carry the digits: V = t3 2^96 + L, L = w2 2^64 + w1 2^32 + w0 with 0 <= w < 2^32
+    const long long M = 0xffffffffll;
+    long long t = d0;
+    const unsigned long long w0 = (unsigned long long)(t & M);
+    t = d1 + (t >> 32);
+    const unsigned long long w1 = (unsigned long long)(t & M);
+    t = d2 + (t >> 32);
+    unsigned long long lhi = (unsigned long long)(t & M);  // L = lhi 2^64 + llo
+    unsigned long long llo = (w1 << 32) | w0;
+    long long top = d3 + (t >> 32);
+    double sign = 1.0;
+    if (top < 0) {
+        // |V| = (-top - 1) 2^96 + (2^96 - L), or -top 2^96 when L = 0
+        sign = -1.0;
+        if (lhi == 0ull && llo == 0ull) {
+            top = -top;
         } else {
-            pl[r0][col - kIcpVals] = h + l;
+            top = -top - 1;
+            const unsigned long long borrow = llo != 0ull ? 1ull : 0ull;
+            llo = ~llo + 1ull;
+            lhi = ((1ull << 32) - lhi - borrow) & 0xffffffffull;
         }
     }
-    __syncthreads();
-    if (t < kIcpVals) {
-        float H = 0.f, L = 0.f;
-        for (int q = 0; q < kLanes; ++q) {
-            float sum, e;
-            two_sum(H, ph[q][t], sum, e);
-            H = sum;
-            L += (e + pc[q][t]) + pl[q][t];
+    // non-negative terms from the top: a relative error of a few ulps, no cancellation
+    double v = (double)top * 0x1p96;
+    v += (double)lhi * 0x1p64;
+    v += (double)llo;
+    return sign * v * 0x1p-48;
+}
+
+}  // namespace fix
+
+// Sums each of the 28 values over the warp; lane l < 28 returns the sum of value l.  A
+// butterfly in which every exchange halves the values a lane carries: 16 + 8 + 4 + 2 + 1
+// shuffles in all, where a sum per value and level takes 28 per level.
+__device__ __forceinline__ float warp_sum_transposed(const float (&v)[kIcpVals])
+{
+    const int lane = threadIdx.x & 31;
+    float a[16];
+    {
+        const bool up = lane & 16;
+#pragma unroll
+        for (int k = 0; k < 16; ++k) {
+            const float lo = v[k], hi = k + 16 < kIcpVals ? v[k + 16] : 0.f;
+            a[k] = (up ? hi : lo) + __shfl_xor_sync(0xffffffffu, up ? lo : hi, 16);
         }
-        red_hi[t] = H;
-        red_lo[t] = L;
     }
-    __syncthreads();
+#pragma unroll
+    for (int w = 8; w >= 1; w >>= 1) {
+        const bool up = lane & w;
+#pragma unroll
+        for (int k = 0; k < w; ++k) {
+            const float lo = a[k], hi = a[k + w];
+            a[k] = (up ? hi : lo) + __shfl_xor_sync(0xffffffffu, up ? lo : hi, w);
+        }
+    }
+    return a[0];
 }
 
 template <int MODE>
 __global__ void __launch_bounds__(kExactWarps * 32, 4) icp_precise_kernel(
     const float4* __restrict__ vmap, const float4* __restrict__ nmap, const float4* __restrict__ pv,
     const float4* __restrict__ pn, Camera cam, IcpParams prm, const float* Fsrc, const float* Tsrc, State* st,
-    float* __restrict__ partials, int ngroups, int32_t* __restrict__ pair, float* sums_out)
+    long long* __restrict__ fixacc, int ngroups, int32_t* __restrict__ pair, float* sums_out)
 {
     wait_for_producer();
     __shared__ float sF[16], sT[16];
     __shared__ float wsum[kExactWarps][kIcpVals];
-    __shared__ float red_hi[kIcpVals], red_lo[kIcpVals];
     __shared__ int is_last;
     if (threadIdx.x < 16) {
         sF[threadIdx.x] = Fsrc[threadIdx.x];
@@ -764,16 +863,10 @@ __global__ void __launch_bounds__(kExactWarps * 32, 4) icp_precise_kernel(
         }
         if (ok[0]) add_terms(v, a[0], b[0]);
         if (ok[1]) add_terms(v, a[1], b[1]);
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1)
-#pragma unroll
-            for (int k = 0; k < kIcpVals; ++k) v[k] = v[k] + __shfl_xor_sync(0xffffffffu, v[k], off);
     }
-    if (lane == 0)
-#pragma unroll
-        for (int k = 0; k < kIcpVals; ++k) wsum[warp][k] = v[k];
+    const float vs = warp_sum_transposed(v);  // the whole warp: also where grp >= ngroups
+    if (lane < kIcpVals) wsum[warp][lane] = vs;
     __syncthreads();
-    const int nblocks = gridDim.x;
     if (threadIdx.x < kIcpVals) {
         const int k = threadIdx.x;
         float h = wsum[0][k], l = 0.f;
@@ -783,41 +876,25 @@ __global__ void __launch_bounds__(kExactWarps * 32, 4) icp_precise_kernel(
             h = sum;
             l += e;
         }
-        partials[(size_t)blockIdx.x * 2 * kIcpVals + k] = h;
-        partials[(size_t)blockIdx.x * 2 * kIcpVals + kIcpVals + k] = l;
+        fix::accumulate(fixacc, &st->fix_bad, k, blockIdx.x % fix::kFixReplicas, h, l);
         __threadfence();
     }
-    // level 1: the slab's last block adds the slab's block partials
-    const int slab_size = max(kSlabRows, (nblocks + kMaxSlabs - 1) / kMaxSlabs);
-    const int slab = blockIdx.x / slab_size, nslabs = (nblocks + slab_size - 1) / slab_size;
-    const int slab_lo = slab * slab_size, slab_n = min(slab_size, nblocks - slab_lo);
     __syncthreads();
-    if (threadIdx.x == 0) is_last = atomicAdd(&st->slab_ticket[slab], 1u) == (unsigned)slab_n - 1;
+    if (threadIdx.x == 0) is_last = atomicAdd(&st->ticket, 1u) == gridDim.x - 1;
     __syncthreads();
     if (!is_last) return;
     __threadfence();
-    reduce_rows(partials + (size_t)slab_lo * 2 * kIcpVals, slab_n, red_hi, red_lo);
-    float* slab_part = partials + (size_t)nblocks * 2 * kIcpVals;
-    if (threadIdx.x < kIcpVals) {
-        slab_part[(size_t)slab * 2 * kIcpVals + threadIdx.x] = red_hi[threadIdx.x];
-        slab_part[(size_t)slab * 2 * kIcpVals + kIcpVals + threadIdx.x] = red_lo[threadIdx.x];
-        __threadfence();
-    }
-    if (threadIdx.x == 0) st->slab_ticket[slab] = 0u;
-    __syncthreads();
-    // level 2: the last slab adds the slab partials and finishes the iteration
-    if (threadIdx.x == 0) is_last = atomicAdd(&st->ticket, 1u) == (unsigned)nslabs - 1;
-    __syncthreads();
-    if (!is_last) return;
-    __threadfence();
-    reduce_rows(slab_part, nslabs, red_hi, red_lo);
-    if (threadIdx.x == 0) st->ticket = 0u;
+    __shared__ long long digits[kIcpVals * 4];
+    fix::gather_digits(fixacc, digits);
     if (threadIdx.x >= 32) return;
+    const unsigned bad = atomicExch(&st->fix_bad, 0u);
+    const double val = lane < kIcpVals ? fix::take(digits, lane, (bad >> lane) & 1u) : 0.0;
+    if (lane == 0) st->ticket = 0u;
     if (MODE == 1) {
-        if (lane < kIcpVals) sums_out[lane] = red_hi[lane] + red_lo[lane];
+        if (lane < kIcpVals) sums_out[lane] = (float)val;
         return;
     }
-    finish_precise_warp(st, prm, red_hi, red_lo);
+    finish_precise_warp(st, prm, val);
 }
 
 template <int MODE>
@@ -871,13 +948,13 @@ int icp_groups(int H, int W) { return (H * W + 63) / 64; }
 
 void icp_prepare(int H, int W) { ensure_solve_smem(icp_groups(H, W)); }
 
+size_t icp_fixacc_words() { return (size_t)kIcpVals * 4 * fix::kFixReplicas * 16; }
+
 size_t icp_scratch_floats(int H, int W)
 {
     const size_t a = (size_t)2 * blocks_for(H, W) * kIcpVals;
     const size_t b = (size_t)icp_groups(H, W) * kIcpVals;
-    // the precision form: block partials then slab partials, hi/lo each
-    const size_t c = (size_t)2 * kIcpVals * ((icp_groups(H, W) + kExactWarps - 1) / kExactWarps + kMaxSlabs);
-    return a > b ? (a > c ? a : c) : (b > c ? b : c);
+    return a > b ? a : b;
 }
 
 namespace {
@@ -890,7 +967,7 @@ int exact_blocks(int H, int W)
 
 void launch_icp_iteration(const float4* vmap, const float4* nmap, const float4* pv, const float4* pn,
                           const Camera& cam, const IcpParams& prm, State* st, float* partials, int* list,
-                          cudaStream_t s)
+                          long long* fixacc, cudaStream_t s)
 {
     const int blocks = blocks_for(cam.H, cam.W);
     if (!prm.precise && prm.reference_order) {
@@ -903,7 +980,7 @@ void launch_icp_iteration(const float4* vmap, const float4* nmap, const float4* 
     } else if (prm.precise) {
         const int ng = icp_groups(cam.H, cam.W);
         launch_pdl(icp_precise_kernel<0>, dim3(exact_blocks(cam.H, cam.W)), dim3(kExactWarps * 32), 0, s, vmap, nmap,
-                   pv, pn, cam, prm, state_F(st), state_T(st), st, partials, ng, (int32_t*)nullptr, (float*)nullptr);
+                   pv, pn, cam, prm, state_F(st), state_T(st), st, fixacc, ng, (int32_t*)nullptr, (float*)nullptr);
     } else
         icp_kernel<false, 0><<<blocks, kIcpBlock, 0, s>>>(vmap, nmap, pv, pn, cam, prm, st, state_F(st),
                                                           state_T(st), partials, nullptr, nullptr);
@@ -911,7 +988,8 @@ void launch_icp_iteration(const float4* vmap, const float4* nmap, const float4* 
 
 void launch_icp_associate(const float4* vmap, const float4* nmap, const float4* pv, const float4* pn,
                           const Camera& cam, const IcpParams& prm, const float* F, const float* T, State* st,
-                          float* partials, int* list, float* sums_out, int32_t* pair, cudaStream_t s)
+                          float* partials, int* list, long long* fixacc, float* sums_out, int32_t* pair,
+                          cudaStream_t s)
 {
     const int blocks = blocks_for(cam.H, cam.W);
     if (!prm.precise && prm.reference_order) {
@@ -924,7 +1002,7 @@ void launch_icp_associate(const float4* vmap, const float4* nmap, const float4* 
     } else if (prm.precise) {
         const int ng = icp_groups(cam.H, cam.W);
         launch_pdl(icp_precise_kernel<1>, dim3(exact_blocks(cam.H, cam.W)), dim3(kExactWarps * 32), 0, s, vmap, nmap,
-                   pv, pn, cam, prm, F, T, st, partials, ng, pair, sums_out);
+                   pv, pn, cam, prm, F, T, st, fixacc, ng, pair, sums_out);
     } else
         icp_kernel<false, 1><<<blocks, kIcpBlock, 0, s>>>(vmap, nmap, pv, pn, cam, prm, st, F, T, partials,
                                                           sums_out, pair);

@@ -33,14 +33,18 @@ int icp_groups(int H, int W);
 // shared-memory limit of the reduce-and-solve kernel
 void icp_prepare(int H, int W);
 size_t icp_scratch_floats(int H, int W);
+// the precision form's fixed-point accumulators: this many zero-initialised 64-bit words
+// (zero again after every launch)
+size_t icp_fixacc_words();
 void launch_icp_iteration(const float4* vmap, const float4* nmap, const float4* pv, const float4* pn,
                           const Camera& cam, const IcpParams& prm, State* st, float* partials, int* list,
-                          cudaStream_t s);
+                          long long* fixacc, cudaStream_t s);
 // Association + reduction only at the given F, T (device pointers to 16 floats each);
 // sums_out receives kIcpVals floats (27 sums + count), pair may be nullptr.
 void launch_icp_associate(const float4* vmap, const float4* nmap, const float4* pv, const float4* pn,
                           const Camera& cam, const IcpParams& prm, const float* F, const float* T, State* st,
-                          float* partials, int* list, float* sums_out, int32_t* pair, cudaStream_t s);
+                          float* partials, int* list, long long* fixacc, float* sums_out, int32_t* pair,
+                          cudaStream_t s);
 
 // per-pixel integration table + T^-1 and the in-front axis into st
 // the integration table (per pixel) and, after its H*W entries, the 8x8-tile depth

@@ -114,6 +114,6 @@ extern "C" kf_status kf_icp_associate_noalloc(int height, int width, const float
                              reinterpret_cast<const float4*>(pred_v), reinterpret_cast<const float4*>(pred_n), cam,
                              prm, mats, mats + 16, reinterpret_cast<kf::State*>(base + kStateOff),
                              reinterpret_cast<float*>(base + kPartialsOff), reinterpret_cast<int*>(base + kListOff),
-                             sums28, pair, s);
+                             nullptr, sums28, pair, s);
     return cudaGetLastError() == cudaSuccess ? KF_OK : KF_ERR_CUDA;
 }

@@ -102,7 +102,44 @@ __global__ void __launch_bounds__(kWarps * 32) selftest_kernel(uint64_t seed, in
     atomicAdd(&counts[4], badm);
 }
 
+// one warp per system: lane c < 6 takes column c of A, lane 6 takes b
+__global__ void __launch_bounds__(kWarps * 32) solve6_kernel(const double* __restrict__ A,
+                                                             const double* __restrict__ b, double* __restrict__ x,
+                                                             int* __restrict__ ok, int n)
+{
+    const int sys = blockIdx.x * kWarps + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    if (sys >= n) return;  // the same in the whole warp
+    double col[6];
+    for (int i = 0; i < 6; ++i)
+        col[i] = lane < 6 ? A[(size_t)sys * 36 + i * 6 + lane] : lane == 6 ? b[(size_t)sys * 6 + i] : 0.0;
+    const bool solved = kf::warp_gj6_f64(col);
+    if (lane == 6 && solved)
+        for (int i = 0; i < 6; ++i) x[(size_t)sys * 6 + i] = col[i];
+    if (lane == 0) ok[sys] = solved ? 1 : 0;
+}
+
 }  // namespace
+
+extern "C" kf_status kf_selftest_solve6(const double* A, const double* b, double* x, int* ok, int n)
+{
+    if (!A || !b || !x || !ok || n <= 0 || n > (1 << 20)) return KF_ERR_INVALID_ARGUMENT;
+    double* d = nullptr;
+    const size_t nd = (size_t)n * (36 + 6 + 6);
+    if (cudaMalloc(&d, nd * sizeof(double) + (size_t)n * sizeof(int)) != cudaSuccess) return KF_ERR_CUDA;
+    double *dA = d, *db = d + (size_t)n * 36, *dx = db + (size_t)n * 6;
+    int* dok = (int*)(d + nd);
+    cudaError_t e = cudaMemcpy(dA, A, (size_t)n * 36 * sizeof(double), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(db, b, (size_t)n * 6 * sizeof(double), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(dx, x, (size_t)n * 6 * sizeof(double), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        solve6_kernel<<<(n + kWarps - 1) / kWarps, kWarps * 32>>>(dA, db, dx, dok, n);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(x, dx, (size_t)n * 6 * sizeof(double), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(ok, dok, (size_t)n * sizeof(int), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    return e == cudaSuccess ? KF_OK : KF_ERR_CUDA;
+}
 
 extern "C" kf_status kf_selftest_solve(unsigned long long seed, int blocks, int systems_per_warp,
                                        unsigned long long counts[5])

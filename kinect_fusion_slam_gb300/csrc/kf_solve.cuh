@@ -286,60 +286,73 @@ __device__ __forceinline__ float mat4_entry(const float* a, const float* b, int 
     return ff::mat4_entry_f64(a, b, r, c);
 }
 
-// The precision form's solve: A x = b in FP64 by the calling warp (all 32 lanes call),
-// a Cholesky factor formed column by column (pivot by lane j, its column by lanes
-// j+1..5, each entry's terms as FMAs in k order), the reciprocal pivots from the FP64
-// rsqrt, and both substitutions column-oriented so that each step is one FMA per lane.
-// A: 6x6 shared doubles, lower triangle on entry, the factor on return; x: 6 shared
-// doubles, b on entry, the solution on return when A is positive definite (else false
-// and x untouched).  r: 6 shared doubles of scratch.
-__device__ __forceinline__ bool warp_chol6_f64(double* A, double* x, double* r, int* fail)
+// Division by the pivot in the Gauss-Jordan steps: q = a / p for p > 0 in
+// [2^-1000, 2^1000].  y0 = rcp.approx.ftz.f64(p) has a relative error e0 = 1 - p y0
+// of about 2^-20 (kf_selftest_solve6 checks the solves built on this); then
+// a / p = a y0 / (1 - e0) = a y0 (1 + e0 + e0^2 + e0^3 + ...), and the first three terms
+// leave a relative error e0^3 ~ 2^-60, below FP64 rounding.  a y0 and e0 are independent,
+// so the dependent chain is the approximation and three FP64 operations (FP64 latency
+// is ~64 cycles per operation on this part).
+__device__ __forceinline__ double div_pivot(double a, double p)
 {
-    const int lane = threadIdx.x & 31;
-    if (lane == 0) *fail = 0;
-    __syncwarp();
+    double y0;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y0) : "d"(p));
+    const double q0 = a * y0;
+    const double e0 = fma(-p, y0, 1.0);
+    const double t = fma(e0, e0, e0);
+    return fma(q0, t, q0);
+}
+
+// The precision form's solve: A x = b in FP64 by the calling warp (all 32 lanes call)
+// for a symmetric A, by Gauss-Jordan elimination of [A | b] without pivoting.  For a
+// positive definite A the pivots are the successive Schur complements, all positive
+// (they are the squares of the Cholesky factor's diagonal); a pivot that is not > 0 is
+// Cholesky's failure test, and the solve reports false.  Lane c < 6 holds column c of A
+// and lane 6 holds b (col[i] = row i); after the six steps lane 6 holds A^-1 b.  The
+// steps run without a branch (a step's critical path is the pivot's shuffle, its
+// division and one update); the pivots are checked afterwards, and the rare system
+// whose pivots fall outside div_pivot's range is solved again with IEEE divisions.
+__device__ __forceinline__ bool warp_gj6_f64(double (&col)[6])
+{
+    double in[6], piv[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) in[i] = col[i];
+#pragma unroll
     for (int j = 0; j < 6; ++j) {
-        double s = 0.0;
-        if (lane >= j && lane < 6) {
-            s = A[lane * 6 + j];
-            for (int k = 0; k < j; ++k) s = fma(-A[lane * 6 + k], A[j * 6 + k], s);
-        }
-        if (lane == j) {
-            if (!(s > 0.0))
-                *fail = 1;
-            else {
-                const double q = rsqrt(s);
-                r[j] = q;
-                A[j * 6 + j] = s * q;
-            }
-        }
-        __syncwarp();
-        if (*fail) return false;
-        if (lane > j && lane < 6) A[lane * 6 + j] = s * r[j];
-        __syncwarp();
+        const double p = __shfl_sync(0xffffffffu, col[j], j);
+        piv[j] = p;
+        double m[6];
+#pragma unroll
+        for (int i = 0; i < 6; ++i) m[i] = __shfl_sync(0xffffffffu, col[i], j);
+        const double aj = div_pivot(col[j], p);
+#pragma unroll
+        for (int i = 0; i < 6; ++i)
+            if (i != j) col[i] = fma(-m[i], aj, col[i]);
+        col[j] = aj;
     }
-    // forward: y_i = (b_i - sum_k L_ik y_k) / L_ii, lanes i > k subtract as y_k appears
-    double v = lane < 6 ? x[lane] : 0.0;
-    for (int k = 0; k < 6; ++k) {
-        if (lane == k) {
-            v = v * r[k];
-            x[k] = v;
-        }
-        __syncwarp();
-        if (lane > k && lane < 6) v = fma(-A[lane * 6 + k], x[k], v);
+    bool pd = true, in_range = true;
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+        pd = pd && piv[j] > 0.0;
+        in_range = in_range && piv[j] > 0x1p-1000 && piv[j] < 0x1p1000;
     }
-    __syncwarp();
-    // backward: x_i = (y_i - sum_{k>i} L_ki x_k) / L_ii
-    v = lane < 6 ? x[lane] : 0.0;
-    for (int k = 5; k >= 0; --k) {
-        if (lane == k) {
-            v = v * r[k];
-            x[k] = v;
-        }
-        __syncwarp();
-        if (lane < k) v = fma(-A[k * 6 + lane], x[k], v);
+    if (!pd) return false;  // the same in every lane
+    if (in_range) return true;
+#pragma unroll
+    for (int i = 0; i < 6; ++i) col[i] = in[i];
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+        const double p = __shfl_sync(0xffffffffu, col[j], j);
+        if (!(p > 0.0)) return false;
+        double m[6];
+#pragma unroll
+        for (int i = 0; i < 6; ++i) m[i] = __shfl_sync(0xffffffffu, col[i], j);
+        const double aj = col[j] / p;
+#pragma unroll
+        for (int i = 0; i < 6; ++i)
+            if (i != j) col[i] = fma(-m[i], aj, col[i]);
+        col[j] = aj;
     }
-    __syncwarp();
     return true;
 }
 

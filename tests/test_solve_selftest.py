@@ -8,6 +8,7 @@ singular) and counts differences.
 """
 import ctypes as C
 
+import numpy as np
 import pytest
 
 from kinect_fusion_slam_gb300 import _lib
@@ -33,3 +34,52 @@ def test_selftest_rejects_bad_arguments():
     counts = (C.c_ulonglong * 5)()
     assert lib.kf_selftest_solve(1, 0, 64, counts) == _lib.KF_ERR_INVALID_ARGUMENT
     assert lib.kf_selftest_solve(1, 4, 64, None) == _lib.KF_ERR_INVALID_ARGUMENT
+
+
+def _icp_like_systems(rng, n):
+    """Sums of rows a = (v x m, m) with v up to a few metres (mm) and unit m over 3 to
+    400 rows -- the shape of the ICP's normal equations; the short ones are singular."""
+    A = np.zeros((n, 6, 6))
+    b = np.zeros((n, 6))
+    for k in range(n):
+        rows = int(rng.choice([3, 5, 6, 8, 64, 400]))
+        scale = 1.0 + 3000.0 * rng.random()
+        v = scale * np.column_stack([rng.uniform(-1, 1, rows), rng.uniform(-1, 1, rows),
+                                     rng.uniform(1.0, 2.0, rows)])
+        m = rng.normal(size=(rows, 3))
+        m /= np.linalg.norm(m, axis=1, keepdims=True)
+        a = np.hstack([np.cross(v, m), m])
+        r = 20.0 * rng.uniform(-1, 1, rows)
+        A[k] = a.T @ a
+        b[k] = a.T @ r
+    return A, b
+
+
+def test_fp64_solve_against_numpy():
+    """The precision form's FP64 warp solve (Gauss-Jordan with Newton-refined pivot
+    reciprocals) against numpy's FP64 Cholesky solve: the same positive-definite
+    decision away from the boundary, and solutions within 1e-12 relative (scaled by the
+    system's condition number) where it solves."""
+    rng = np.random.default_rng(7)
+    n = 4096
+    A, b = _icp_like_systems(rng, n)
+    x = np.zeros((n, 6))
+    ok = np.zeros(n, np.int32)
+    lib = _lib.load()
+    st = lib.kf_selftest_solve6(A.ctypes.data, b.ctypes.data, x.ctypes.data, ok.ctypes.data, n)
+    assert st == _lib.KF_OK
+    n_pd = 0
+    for k in range(n):
+        w = np.linalg.eigvalsh(A[k])
+        ratio = w[0] / w[-1]
+        if abs(ratio) < 1e-13:
+            continue  # at the positive-definite boundary either decision is rounding
+        pd = ratio > 0
+        assert bool(ok[k]) == pd, (k, ratio)
+        if pd:
+            n_pd += 1
+            xr = np.linalg.solve(A[k], b[k])
+            err = np.linalg.norm(x[k] - xr) / max(np.linalg.norm(xr), 1e-300)
+            assert err <= 1e-12 / ratio + 1e-14, (k, err, ratio)
+    assert n_pd > 0.5 * n
+    assert (ok == 0).sum() > 0.05 * n
