@@ -300,8 +300,9 @@ kf_status kf_kernels_per_frame(kf_handle* h, int* n);
  * not positive definite, [4] differing product entries.  Synchronous. */
 kf_status kf_selftest_solve(unsigned long long seed, int blocks, int systems_per_warp,
                             unsigned long long counts[5]);
-/* The precision form's FP64 warp solve (Gauss-Jordan on [A | b], stopping at a pivot
- * that is not > 0) on n systems given in host memory: A (n x 36 doubles, row-major,
+/* The precision form's FP64 solve (fraction-free Gauss-Jordan on [A | b] by a warp
+ * pair, a pivot that is not > 0 meaning not positive definite) on n systems given in
+ * host memory: A (n x 36 doubles, row-major,
  * symmetric), b (n x 6); writes x (n x 6, untouched where not solved) and ok (n: 1
  * solved, 0 not positive definite).  n <= 1 << 20.  Synchronous. */
 kf_status kf_selftest_solve6(const double* A, const double* b, double* x, int* ok, int n);

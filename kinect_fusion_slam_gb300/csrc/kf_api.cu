@@ -173,10 +173,13 @@ void enq_icp(kf_handle* h)
         launch_pyramid_prediction(h->d_pv_l[l - 1], h->d_pn_l[l - 1], f.W, h->d_pv_l[l], h->d_pn_l[l], c.H, c.W,
                                   h->stream);
     }
+    bool after_pass = false;  // the previous launch in the stream is an ICP pass
     for (int l = L - 1; l >= 0; --l)
-        for (int it = 0; it < h->cfg.icp_iterations[l]; ++it)
+        for (int it = 0; it < h->cfg.icp_iterations[l]; ++it) {
             launch_icp_iteration(h->d_vmap_l[l], h->d_nmap_l[l], h->d_pv_l[l], h->d_pn_l[l], h->lcam[l], h->icp,
-                                 h->d_state, h->d_partials, h->d_groups, h->d_fixacc, h->stream);
+                                 h->d_state, h->d_partials, h->d_groups, h->d_fixacc, after_pass, h->stream);
+            after_pass = true;
+        }
 }
 
 void enq_integrate(kf_handle* h, bool first)

@@ -130,21 +130,28 @@ __device__ __forceinline__ bool associate(int i, const float4* __restrict__ vmap
 // that each round of loads is issued for both pixels before either is used -- the
 // vertices and normals together, then both matched predictions -- which turns six
 // dependent L2 round trips into two.  The arithmetic is associate()'s, operation for
-// operation; only independent loads move.
-__device__ __forceinline__ void associate_pair(int i0, int n, const float4* __restrict__ vmap,
-                                               const float4* __restrict__ nmap, const float4* __restrict__ pv,
-                                               const float4* __restrict__ pn, const Camera& cam, const float* F,
-                                               const float* T, float dist_th, float ang_th, bool (&ok)[2],
-                                               float (&a)[2][6], float (&b)[2], int (&j)[2])
+// operation; only independent loads move.  load_pair is the first round of loads
+// (the lane's two vertices and normals, zero past the image), associate_pair_from the
+// rest.
+__device__ __forceinline__ void load_pair(int i0, int n, const float4* __restrict__ vmap,
+                                          const float4* __restrict__ nmap, float4 (&v)[2], float4 (&nn)[2])
 {
     const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
-    float4 v[2], nn[2];
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
         const int i = i0 + 32 * h;
         v[h] = i < n ? vmap[i] : zero;
         nn[h] = i < n ? nmap[i] : zero;
     }
+}
+
+__device__ __forceinline__ void associate_pair_from(const float4 (&v)[2], const float4 (&nn)[2],
+                                                    const float4* __restrict__ pv, const float4* __restrict__ pn,
+                                                    const Camera& cam, const float* F, const float* T, float dist_th,
+                                                    float ang_th, bool (&ok)[2], float (&a)[2][6], float (&b)[2],
+                                                    int (&j)[2])
+{
+    const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
     float3 g[2];
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
@@ -160,6 +167,17 @@ __device__ __forceinline__ void associate_pair(int i0, int n, const float4* __re
 #pragma unroll
     for (int h = 0; h < 2; ++h)
         if (ok[h]) ok[h] = assoc_finish(g[h], nn[h], q[h], m[h], T, dist_th, ang_th, a[h], b[h]);
+}
+
+__device__ __forceinline__ void associate_pair(int i0, int n, const float4* __restrict__ vmap,
+                                               const float4* __restrict__ nmap, const float4* __restrict__ pv,
+                                               const float4* __restrict__ pn, const Camera& cam, const float* F,
+                                               const float* T, float dist_th, float ang_th, bool (&ok)[2],
+                                               float (&a)[2][6], float (&b)[2], int (&j)[2])
+{
+    float4 v[2], nn[2];
+    load_pair(i0, n, vmap, nmap, v, nn);
+    associate_pair_from(v, nn, pv, pn, cam, F, T, dist_th, ang_th, ok, a, b, j);
 }
 
 // Deterministic block reduction: butterfly shuffles within each warp, then warp
@@ -252,40 +270,35 @@ __device__ void finish_iteration_warp(State* st, const IcpParams& prm, const flo
     }
 }
 
-// The precision form's update by one warp: the sums as FP64 (lane k < kIcpVals holds
-// sum k: b, then A's upper triangle by rows, then the correspondence count), the FP64
-// solve (warp_gj6_f64), and the SE(3) composition Inc * T applied to the FP64 pose (the
+// The precision form's update by the first two warps of the last block (threads 0..63
+// call; S: the sums as FP64 in shared memory, sum k: b, then A's upper triangle by rows,
+// then the correspondence count): the FP64 solve (pair_gj6_f64 on named barriers 1 and
+// 2), and the SE(3) composition Inc * T applied to the FP64 pose by the first warp (the
 // only FP64 steps); the float pose and F follow from it.  The previous pose is loaded
 // first so that its latency hides behind the solve.
-__device__ void finish_precise_warp(State* st, const IcpParams& prm, double val)
+__device__ void finish_precise_pair(State* st, const IcpParams& prm, const double* S)
 {
+    __shared__ double gj_buf[2][6][8], gj_x[6];
     __shared__ float Tf[16], Tp[16];
-    const int lane = threadIdx.x & 31;
+    const int t = threadIdx.x, lane = t & 31;
+    const float tp = t < 16 ? st->Tprev_inv[t] : 0.f;
+    const double td = t < 16 ? st->Td[t] : 0.0;
+    const auto entry = [S](int r, int c) { return c == 6 ? S[r] : S[tri(min(r, c), max(r, c))]; };
+    const bool ok = pair_gj6_f64(entry, t, gj_buf, gj_x, 1);
+    if (t >= 32) return;
     const int it = st->iter;
-    const float tp = lane < 16 ? st->Tprev_inv[lane] : 0.f;
-    const double td = lane < 16 ? st->Td[lane] : 0.0;
-    if (lane < kIcpVals) st->sums[lane] = (float)val;
-    // lane c < 6: column c of A; lane 6: b
-    double col[6], b[6];
-#pragma unroll
-    for (int i = 0; i < 6; ++i) {
-        const int src = lane < 6 ? tri(min(i, lane), max(i, lane)) : i;
-        col[i] = __shfl_sync(0xffffffffu, val, src);
-        b[i] = col[i];
-    }
-    const bool ok = warp_gj6_f64(col);
-    const double count = __shfl_sync(0xffffffffu, val, kIcpVals - 1);
+    if (lane < kIcpVals) st->sums[lane] = (float)S[lane];
     // the increment (omega, t) in every lane; where A is not positive definite the
     // reference applies b as it stands, or the identity in that fail mode
     double x[6];
 #pragma unroll
-    for (int i = 0; i < 6; ++i) x[i] = __shfl_sync(0xffffffffu, ok ? col[i] : (prm.fail_mode == 1 ? 0.0 : b[i]), 6);
+    for (int i = 0; i < 6; ++i) x[i] = ok ? gj_x[i] : (prm.fail_mode == 1 ? 0.0 : S[i]);
     // row rr of Inc = [[1, w2, -w1, t0], [-w2, 1, w0, t1], [w1, -w0, 1, t2], [0, 0, 0, 1]]
     const int rr = (lane >> 2) & 3, c = lane & 3;
     const double i0 = rr == 0 ? 1.0 : rr == 1 ? -x[2] : rr == 2 ? x[1] : 0.0;
     const double i1 = rr == 0 ? x[2] : rr == 1 ? 1.0 : rr == 2 ? -x[0] : 0.0;
     const double i2 = rr == 0 ? -x[1] : rr == 1 ? x[0] : rr == 2 ? 1.0 : 0.0;
-    const double i3 = rr == 3 ? 1.0 : x[3 + rr];
+    const double i3 = rr == 0 ? x[3] : rr == 1 ? x[4] : rr == 2 ? x[5] : 1.0;
     const double t0 = __shfl_sync(0xffffffffu, td, c), t1 = __shfl_sync(0xffffffffu, td, 4 + c);
     const double t2 = __shfl_sync(0xffffffffu, td, 8 + c), t3 = __shfl_sync(0xffffffffu, td, 12 + c);
     double tn = i0 * t0;
@@ -306,7 +319,7 @@ __device__ void finish_precise_warp(State* st, const IcpParams& prm, double val)
     }
     if (lane == 0) {
         if (it < kMaxIcpIters) {
-            st->ncorr[it] = (int32_t)count;
+            st->ncorr[it] = (int32_t)S[kIcpVals - 1];
             st->chol_ok[it] = ok ? 1 : 0;
         }
         st->iter = it + 1;
@@ -315,7 +328,7 @@ __device__ void finish_precise_warp(State* st, const IcpParams& prm, double val)
 
 // MODE 0: one ICP iteration (F, T from the state; the last block updates the pose).
 // MODE 1: association + reduction at the given F, T; the last block writes the sums.
-template <bool PRECISE, int MODE>
+template <int MODE>
 __global__ void __launch_bounds__(kIcpBlock) icp_kernel(const float4* __restrict__ vmap, const float4* __restrict__ nmap,
                                                       const float4* __restrict__ pv, const float4* __restrict__ pn,
                                                       Camera cam, IcpParams prm, State* st, const float* Fsrc,
@@ -324,7 +337,7 @@ __global__ void __launch_bounds__(kIcpBlock) icp_kernel(const float4* __restrict
 {
     __shared__ float sF[16], sT[16];
     __shared__ float sh_hi[(kIcpBlock / 32) * kIcpVals];
-    __shared__ float sh_lo[PRECISE ? (kIcpBlock / 32) * kIcpVals : 1];
+    __shared__ float sh_lo[1];
     __shared__ float red_hi[kIcpVals], red_lo[kIcpVals];
     __shared__ int is_last;
     if (threadIdx.x < 16) {
@@ -333,7 +346,7 @@ __global__ void __launch_bounds__(kIcpBlock) icp_kernel(const float4* __restrict
     }
     __syncthreads();
 
-    Acc<PRECISE> acc;
+    Acc<false> acc;
     acc.zero();
     const int n = cam.H * cam.W;
     for (int i = blockIdx.x * kIcpBlock + threadIdx.x; i < n; i += gridDim.x * kIcpBlock) {
@@ -350,14 +363,12 @@ __global__ void __launch_bounds__(kIcpBlock) icp_kernel(const float4* __restrict
             for (int s = r; s < 6; ++s) acc.add(tri(r, s), a[r] * a[s]);
         acc.add(kIcpVals - 1, 1.f);
     }
-    block_reduce<PRECISE>(acc, sh_hi, sh_lo, red_hi, red_lo);
+    block_reduce<false>(acc, sh_hi, sh_lo, red_hi, red_lo);
 
     // publish this block's partial; the last block to arrive finishes the reduction
     float* part_hi = partials;
-    float* part_lo = partials + (size_t)gridDim.x * kIcpVals;
     if (threadIdx.x < kIcpVals) {
         part_hi[blockIdx.x * kIcpVals + threadIdx.x] = red_hi[threadIdx.x];
-        if (PRECISE) part_lo[blockIdx.x * kIcpVals + threadIdx.x] = red_lo[threadIdx.x];
         __threadfence();
     }
     __syncthreads();
@@ -370,27 +381,22 @@ __global__ void __launch_bounds__(kIcpBlock) icp_kernel(const float4* __restrict
     for (int bidx = threadIdx.x; bidx < (int)gridDim.x; bidx += kIcpBlock) {
 #pragma unroll
         for (int k = 0; k < kIcpVals; ++k)
-            acc.add_pair(k, __ldcg(part_hi + bidx * kIcpVals + k), PRECISE ? __ldcg(part_lo + bidx * kIcpVals + k) : 0.f);
+            acc.add_pair(k, __ldcg(part_hi + bidx * kIcpVals + k), 0.f);
     }
-    block_reduce<PRECISE>(acc, sh_hi, sh_lo, red_hi, red_lo);
+    block_reduce<false>(acc, sh_hi, sh_lo, red_hi, red_lo);
     if (threadIdx.x >= 32) return;
     if (threadIdx.x == 0) st->ticket = 0u;
     if (MODE == 1) {
-        if (threadIdx.x < kIcpVals) sums_out[threadIdx.x] = PRECISE ? red_hi[threadIdx.x] + red_lo[threadIdx.x] : red_hi[threadIdx.x];
+        if (threadIdx.x < kIcpVals) sums_out[threadIdx.x] = red_hi[threadIdx.x];
         return;
     }
-    if (PRECISE) {
-        const int k = threadIdx.x;
-        finish_precise_warp(st, prm, k < kIcpVals ? (double)red_hi[k] + (double)red_lo[k] : 0.0);
-    } else {
-        __shared__ float sT0[16], sTp[16];
-        if (threadIdx.x < 16) {
-            sT0[threadIdx.x] = st->T[threadIdx.x];
-            sTp[threadIdx.x] = st->Tprev_inv[threadIdx.x];
-        }
-        __syncwarp();
-        finish_iteration_warp(st, prm, red_hi, sT0, sTp, st->iter);
+    __shared__ float sT0[16], sTp[16];
+    if (threadIdx.x < 16) {
+        sT0[threadIdx.x] = st->T[threadIdx.x];
+        sTp[threadIdx.x] = st->Tprev_inv[threadIdx.x];
     }
+    __syncwarp();
+    finish_iteration_warp(st, prm, red_hi, sT0, sTp, st->iter);
 }
 
 // ---- reference summation order ----------------------------------------------------
@@ -740,13 +746,20 @@ __device__ __forceinline__ void accumulate(long long* acc, unsigned* bad, int k,
 
 // The last block's read-out, all threads of the block: each digit's replicas are read
 // (every load issued before any is used), added, and cleared; digits[k * 4 + d] (shared)
-// receives digit d of sum k.
-__device__ __forceinline__ void gather_digits(long long* acc, long long* digits)
+// receives digit d of sum k, and *bad_out (shared) the flags of the sums that could not
+// be accumulated (read and cleared in the same round of loads).
+__device__ __forceinline__ void gather_digits(long long* acc, long long* digits, unsigned* bad_flags,
+                                              unsigned* bad_out)
 {
-    static_assert(kIcpVals * 4 * 2 <= kExactWarps * 32 && kFixReplicas % 2 == 0, "two threads per digit");
+    static_assert(kIcpVals * 4 * 2 < kExactWarps * 32 && kFixReplicas % 2 == 0, "two threads per digit");
     const int t = threadIdx.x, D = t >> 1, half = t & 1;
     constexpr int kPer = kFixReplicas / 2;
     long long v = 0;
+    if (t == kExactWarps * 32 - 1) {
+        // every other block's atomicOr on the flags came before its ticket
+        *bad_out = __ldcg(bad_flags);
+        __stcg(bad_flags, 0u);
+    }
     if (D < kIcpVals * 4) {
         unsigned long long* w[kPer];
         unsigned long long x[kPer];
@@ -835,9 +848,21 @@ template <int MODE>
 __global__ void __launch_bounds__(kExactWarps * 32, 4) icp_precise_kernel(
     const float4* __restrict__ vmap, const float4* __restrict__ nmap, const float4* __restrict__ pv,
     const float4* __restrict__ pn, Camera cam, IcpParams prm, const float* Fsrc, const float* Tsrc, State* st,
-    long long* __restrict__ fixacc, int ngroups, int32_t* __restrict__ pair, float* sums_out)
+    long long* __restrict__ fixacc, int ngroups, int prefetch, int32_t* __restrict__ pair, float* sums_out)
 {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int n = cam.H * cam.W;
+    const int grp = blockIdx.x * kExactWarps + warp;
+    // The vertex and normal maps are written before the frame's first ICP pass and never
+    // by a pass, so after a pass (prefetch) they are loaded before waiting for it: the
+    // first round of loads overlaps the previous pass's solve.
+    float4 v[2], nn[2];
+    if (prefetch) load_pair(grp * 64 + lane, n, vmap, nmap, v, nn);
     wait_for_producer();
+    // the next pass may be scheduled now: it waits for this one to finish before it
+    // reads anything this one writes (every kernel launched with launch_pdl does)
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    if (!prefetch) load_pair(grp * 64 + lane, n, vmap, nmap, v, nn);
     __shared__ float sF[16], sT[16];
     __shared__ float wsum[kExactWarps][kIcpVals];
     __shared__ int is_last;
@@ -846,25 +871,22 @@ __global__ void __launch_bounds__(kExactWarps * 32, 4) icp_precise_kernel(
         sT[threadIdx.x] = Tsrc[threadIdx.x];
     }
     __syncthreads();
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int n = cam.H * cam.W;
-    const int grp = blockIdx.x * kExactWarps + warp;
-    float v[kIcpVals];
+    float vals[kIcpVals];
 #pragma unroll
-    for (int k = 0; k < kIcpVals; ++k) v[k] = 0.f;
+    for (int k = 0; k < kIcpVals; ++k) vals[k] = 0.f;
     if (grp < ngroups) {
         bool ok[2];
         float a[2][6], b[2];
         int j[2];
-        associate_pair(grp * 64 + lane, n, vmap, nmap, pv, pn, cam, sF, sT, prm.dist, prm.angle_deg, ok, a, b, j);
+        associate_pair_from(v, nn, pv, pn, cam, sF, sT, prm.dist, prm.angle_deg, ok, a, b, j);
         if (MODE == 1 && pair) {
             if (grp * 64 + lane < n) pair[grp * 64 + lane] = ok[0] ? j[0] : -1;
             if (grp * 64 + 32 + lane < n) pair[grp * 64 + 32 + lane] = ok[1] ? j[1] : -1;
         }
-        if (ok[0]) add_terms(v, a[0], b[0]);
-        if (ok[1]) add_terms(v, a[1], b[1]);
+        if (ok[0]) add_terms(vals, a[0], b[0]);
+        if (ok[1]) add_terms(vals, a[1], b[1]);
     }
-    const float vs = warp_sum_transposed(v);  // the whole warp: also where grp >= ngroups
+    const float vs = warp_sum_transposed(vals);  // the whole warp: also where grp >= ngroups
     if (lane < kIcpVals) wsum[warp][lane] = vs;
     __syncthreads();
     if (threadIdx.x < kIcpVals) {
@@ -880,21 +902,29 @@ __global__ void __launch_bounds__(kExactWarps * 32, 4) icp_precise_kernel(
         __threadfence();
     }
     __syncthreads();
-    if (threadIdx.x == 0) is_last = atomicAdd(&st->ticket, 1u) == gridDim.x - 1;
+    if (threadIdx.x == 0) {
+        // acquire: the last block's reads of the accumulators come after every block's
+        // additions, which each block fenced before its ticket
+        unsigned old;
+        asm volatile("atom.acquire.gpu.add.u32 %0, [%1], 1;" : "=r"(old) : "l"(&st->ticket) : "memory");
+        is_last = old == gridDim.x - 1;
+    }
     __syncthreads();
     if (!is_last) return;
-    __threadfence();
     __shared__ long long digits[kIcpVals * 4];
-    fix::gather_digits(fixacc, digits);
-    if (threadIdx.x >= 32) return;
-    const unsigned bad = atomicExch(&st->fix_bad, 0u);
-    const double val = lane < kIcpVals ? fix::take(digits, lane, (bad >> lane) & 1u) : 0.0;
-    if (lane == 0) st->ticket = 0u;
+    __shared__ unsigned bad;
+    __shared__ double S[kIcpVals];
+    fix::gather_digits(fixacc, digits, &st->fix_bad, &bad);
+    if (threadIdx.x >= 64) return;
+    const double val = threadIdx.x < kIcpVals ? fix::take(digits, threadIdx.x, (bad >> threadIdx.x) & 1u) : 0.0;
+    if (threadIdx.x == 0) st->ticket = 0u;
     if (MODE == 1) {
-        if (lane < kIcpVals) sums_out[lane] = (float)val;
+        if (threadIdx.x < kIcpVals) sums_out[threadIdx.x] = (float)val;
         return;
     }
-    finish_precise_warp(st, prm, val);
+    if (threadIdx.x < kIcpVals) S[threadIdx.x] = val;
+    pair_bar(1);
+    finish_precise_pair(st, prm, S);
 }
 
 template <int MODE>
@@ -967,7 +997,7 @@ int exact_blocks(int H, int W)
 
 void launch_icp_iteration(const float4* vmap, const float4* nmap, const float4* pv, const float4* pn,
                           const Camera& cam, const IcpParams& prm, State* st, float* partials, int* list,
-                          long long* fixacc, cudaStream_t s)
+                          long long* fixacc, bool after_pass, cudaStream_t s)
 {
     const int blocks = blocks_for(cam.H, cam.W);
     if (!prm.precise && prm.reference_order) {
@@ -980,10 +1010,11 @@ void launch_icp_iteration(const float4* vmap, const float4* nmap, const float4* 
     } else if (prm.precise) {
         const int ng = icp_groups(cam.H, cam.W);
         launch_pdl(icp_precise_kernel<0>, dim3(exact_blocks(cam.H, cam.W)), dim3(kExactWarps * 32), 0, s, vmap, nmap,
-                   pv, pn, cam, prm, state_F(st), state_T(st), st, fixacc, ng, (int32_t*)nullptr, (float*)nullptr);
+                   pv, pn, cam, prm, state_F(st), state_T(st), st, fixacc, ng, after_pass ? 1 : 0, (int32_t*)nullptr,
+                   (float*)nullptr);
     } else
-        icp_kernel<false, 0><<<blocks, kIcpBlock, 0, s>>>(vmap, nmap, pv, pn, cam, prm, st, state_F(st),
-                                                          state_T(st), partials, nullptr, nullptr);
+        icp_kernel<0><<<blocks, kIcpBlock, 0, s>>>(vmap, nmap, pv, pn, cam, prm, st, state_F(st), state_T(st),
+                                                   partials, nullptr, nullptr);
 }
 
 void launch_icp_associate(const float4* vmap, const float4* nmap, const float4* pv, const float4* pn,
@@ -1002,9 +1033,9 @@ void launch_icp_associate(const float4* vmap, const float4* nmap, const float4* 
     } else if (prm.precise) {
         const int ng = icp_groups(cam.H, cam.W);
         launch_pdl(icp_precise_kernel<1>, dim3(exact_blocks(cam.H, cam.W)), dim3(kExactWarps * 32), 0, s, vmap, nmap,
-                   pv, pn, cam, prm, F, T, st, fixacc, ng, pair, sums_out);
+                   pv, pn, cam, prm, F, T, st, fixacc, ng, 0, pair, sums_out);
     } else
-        icp_kernel<false, 1><<<blocks, kIcpBlock, 0, s>>>(vmap, nmap, pv, pn, cam, prm, st, F, T, partials,
+        icp_kernel<1><<<blocks, kIcpBlock, 0, s>>>(vmap, nmap, pv, pn, cam, prm, st, F, T, partials,
                                                           sums_out, pair);
 }
 

@@ -36,9 +36,12 @@ size_t icp_scratch_floats(int H, int W);
 // the precision form's fixed-point accumulators: this many zero-initialised 64-bit words
 // (zero again after every launch)
 size_t icp_fixacc_words();
+// after_pass: the previous launch in the stream is an ICP pass (which writes none of
+// vmap, nmap, pv, pn), so the precision form's pass loads vmap and nmap before waiting
+// for it
 void launch_icp_iteration(const float4* vmap, const float4* nmap, const float4* pv, const float4* pn,
                           const Camera& cam, const IcpParams& prm, State* st, float* partials, int* list,
-                          long long* fixacc, cudaStream_t s);
+                          long long* fixacc, bool after_pass, cudaStream_t s);
 // Association + reduction only at the given F, T (device pointers to 16 floats each);
 // sums_out receives kIcpVals floats (27 sums + count), pair may be nullptr.
 void launch_icp_associate(const float4* vmap, const float4* nmap, const float4* pv, const float4* pn,

@@ -102,20 +102,23 @@ __global__ void __launch_bounds__(kWarps * 32) selftest_kernel(uint64_t seed, in
     atomicAdd(&counts[4], badm);
 }
 
-// one warp per system: lane c < 6 takes column c of A, lane 6 takes b
+// one warp pair per system (pair_gj6_f64), two pairs per block on named barriers 1, 2
+// and 3, 4
 __global__ void __launch_bounds__(kWarps * 32) solve6_kernel(const double* __restrict__ A,
                                                              const double* __restrict__ b, double* __restrict__ x,
                                                              int* __restrict__ ok, int n)
 {
-    const int sys = blockIdx.x * kWarps + (threadIdx.x >> 5), lane = threadIdx.x & 31;
-    if (sys >= n) return;  // the same in the whole warp
-    double col[6];
-    for (int i = 0; i < 6; ++i)
-        col[i] = lane < 6 ? A[(size_t)sys * 36 + i * 6 + lane] : lane == 6 ? b[(size_t)sys * 6 + i] : 0.0;
-    const bool solved = kf::warp_gj6_f64(col);
-    if (lane == 6 && solved)
-        for (int i = 0; i < 6; ++i) x[(size_t)sys * 6 + i] = col[i];
-    if (lane == 0) ok[sys] = solved ? 1 : 0;
+    static_assert(kWarps == 4, "two warp pairs per block");
+    __shared__ double buf[2][2][6][8], xs[2][6];
+    const int pr = threadIdx.x >> 6, t = threadIdx.x & 63;
+    const int sys = blockIdx.x * 2 + pr;
+    if (sys >= n) return;  // the same in the whole pair
+    const double* As = A + (size_t)sys * 36;
+    const double* bs = b + (size_t)sys * 6;
+    const auto entry = [As, bs](int r, int c) { return c == 6 ? bs[r] : As[r * 6 + c]; };
+    const bool solved = kf::pair_gj6_f64(entry, t, buf[pr], xs[pr], 1 + 2 * pr);
+    if (t < 6 && solved) x[(size_t)sys * 6 + t] = xs[pr][t];
+    if (t == 0) ok[sys] = solved ? 1 : 0;
 }
 
 }  // namespace
@@ -132,7 +135,7 @@ extern "C" kf_status kf_selftest_solve6(const double* A, const double* b, double
     if (e == cudaSuccess) e = cudaMemcpy(db, b, (size_t)n * 6 * sizeof(double), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(dx, x, (size_t)n * 6 * sizeof(double), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) {
-        solve6_kernel<<<(n + kWarps - 1) / kWarps, kWarps * 32>>>(dA, db, dx, dok, n);
+        solve6_kernel<<<(n + 1) / 2, kWarps * 32>>>(dA, db, dx, dok, n);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) e = cudaMemcpy(x, dx, (size_t)n * 6 * sizeof(double), cudaMemcpyDeviceToHost);

@@ -303,43 +303,14 @@ __device__ __forceinline__ double div_pivot(double a, double p)
     return fma(q0, t, q0);
 }
 
-// The precision form's solve: A x = b in FP64 by the calling warp (all 32 lanes call)
-// for a symmetric A, by Gauss-Jordan elimination of [A | b] without pivoting.  For a
-// positive definite A the pivots are the successive Schur complements, all positive
-// (they are the squares of the Cholesky factor's diagonal); a pivot that is not > 0 is
-// Cholesky's failure test, and the solve reports false.  Lane c < 6 holds column c of A
-// and lane 6 holds b (col[i] = row i); after the six steps lane 6 holds A^-1 b.  The
-// steps run without a branch (a step's critical path is the pivot's shuffle, its
-// division and one update); the pivots are checked afterwards, and the rare system
-// whose pivots fall outside div_pivot's range is solved again with IEEE divisions.
-__device__ __forceinline__ bool warp_gj6_f64(double (&col)[6])
+// Gauss-Jordan elimination of [A | b] in FP64 by one warp with IEEE divisions, for a
+// symmetric A and without pivoting.  Lane c < 6 holds column c of A and lane 6 holds b
+// (col[i] = row i); after the six steps lane 6 holds A^-1 b.  For a positive definite
+// A the pivots are the successive Schur complements, all positive (the squares of the
+// Cholesky factor's diagonal); a pivot that is not > 0 is Cholesky's failure test and
+// the solve returns false (the same in every lane).  The fallback of pair_gj6_f64.
+__device__ __forceinline__ bool warp_gj6_f64_ieee(double (&col)[6])
 {
-    double in[6], piv[6];
-#pragma unroll
-    for (int i = 0; i < 6; ++i) in[i] = col[i];
-#pragma unroll
-    for (int j = 0; j < 6; ++j) {
-        const double p = __shfl_sync(0xffffffffu, col[j], j);
-        piv[j] = p;
-        double m[6];
-#pragma unroll
-        for (int i = 0; i < 6; ++i) m[i] = __shfl_sync(0xffffffffu, col[i], j);
-        const double aj = div_pivot(col[j], p);
-#pragma unroll
-        for (int i = 0; i < 6; ++i)
-            if (i != j) col[i] = fma(-m[i], aj, col[i]);
-        col[j] = aj;
-    }
-    bool pd = true, in_range = true;
-#pragma unroll
-    for (int j = 0; j < 6; ++j) {
-        pd = pd && piv[j] > 0.0;
-        in_range = in_range && piv[j] > 0x1p-1000 && piv[j] < 0x1p1000;
-    }
-    if (!pd) return false;  // the same in every lane
-    if (in_range) return true;
-#pragma unroll
-    for (int i = 0; i < 6; ++i) col[i] = in[i];
 #pragma unroll
     for (int j = 0; j < 6; ++j) {
         const double p = __shfl_sync(0xffffffffu, col[j], j);
@@ -354,6 +325,114 @@ __device__ __forceinline__ bool warp_gj6_f64(double (&col)[6])
         col[j] = aj;
     }
     return true;
+}
+
+// bar.sync on a named barrier of the 64 threads of a warp pair
+__device__ __forceinline__ void pair_bar(int id) { asm volatile("bar.sync %0, 64;" ::"r"(id) : "memory"); }
+
+// bar.red.or over the warp pair: true in every thread when any thread passes true
+__device__ __forceinline__ bool pair_bar_or(int id, bool v)
+{
+    unsigned out;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\t"
+        "setp.ne.u32 p, %1, 0;\n\t"
+        "bar.red.or.pred q, %2, 64, p;\n\t"
+        "selp.u32 %0, 1, 0, q;\n\t}"
+        : "=r"(out)
+        : "r"((unsigned)v), "r"(id)
+        : "memory");
+    return out != 0u;
+}
+
+// v * 2^(1023 - e), e the exponent field of a normal pivot, by integer arithmetic on
+// v's exponent field (exact where the result is normal).  Zero where v is zero or
+// subnormal or the result would be subnormal (a term below 2^-1022 of the pivot row's
+// scale); `over` is set where the result would overflow or v is not finite.
+__device__ __forceinline__ double scale_by_pivot(double v, int e, bool& over)
+{
+    const int hi = __double2hiint(v), lo = __double2loint(v);
+    const int ev = (hi >> 20) & 0x7ff;
+    const int en = ev - e + 1023;
+    if (ev == 0x7ff || en > 2046) {
+        over = true;
+        return v;
+    }
+    if (ev == 0 || en < 1) return 0.0;
+    return __hiloint2double((hi & 0x800fffff) | (en << 20), lo);
+}
+
+// The precision form's 6x6 solve A x = b in FP64 by a pair of warps (the 64 threads
+// t = threadIdx.x - 64 * pair of one warp pair call; named barriers bar_id and
+// bar_id + 1 are the pair's: bar.sync on the first, bar.red on the second).  A is symmetric; entry(r, c) gives A[r][c] for c < 6 and b[r] for c == 6.
+//
+// This GPU retires one FP64 warp instruction per ~64 cycles per SM sub-partition, so
+// the solve is laid out to put as few of them as possible on its critical path: one
+// entry of [A | b] per thread (warp w holds rows 3w..3w+2, lane l < 21 the entry
+// (3w + l / 7, l % 7)), exchanged through shared memory once per step, and
+// fraction-free Gauss-Jordan steps, row_i <- p' row_i - m'_i row_j for i != j, where p
+// is the pivot a_jj, m_i = a_ij, and p' = p 2^-E, m'_i = m_i 2^-E for E = exponent(p)
+// (exact power-of-two scaling by integer arithmetic on the exponent field, which keeps
+// the entries from growing like products of pivots).  Each step is one FP64 product
+// and one FMA per thread, with no division.  Every row is thereby scaled by positive
+// factors only, so the pivots have the signs of the Schur complements: a pivot that is
+// not > 0 is Cholesky's failure test, and the solve returns false.  After the six
+// steps the A part of row r is diagonal, and x_r = b'_r / a'_rr is one division per row
+// (div_pivot).  A system whose pivots or scaled entries leave the normal range, or
+// whose solution is not finite, is decided and solved again by warp_gj6_f64_ieee.
+//
+// Returns true (in all 64 threads) when A is positive definite; then x[0..5] (shared)
+// holds the solution.  buf: 2 x 6 x 8 shared doubles of scratch.
+template <class Entry>
+__device__ __forceinline__ bool pair_gj6_f64(const Entry& entry, int t, double (*buf)[6][8], double* x, int bar_id)
+{
+    const int w = t >> 5, l = t & 31;
+    const bool act = l < 21;
+    const int r = act ? 3 * w + l / 7 : 0, c = act ? l % 7 : 0;
+    double a = act ? entry(r, c) : 0.0;
+    bool pd = true, bad = false;
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+        double(*M)[8] = buf[j & 1];
+        if (act) M[r][c] = a;
+        pair_bar(bar_id);
+        const double p = M[j][j];
+        const int ep = (__double2hiint(p) >> 20) & 0x7ff;
+        pd = pd && p > 0.0;
+        bad = bad || ep == 0 || ep == 0x7ff;
+        const double ps = scale_by_pivot(p, ep, bad);  // in [1, 2)
+        if (act && r != j) {
+            if (c > j) {
+                const double ms = scale_by_pivot(M[r][j], ep, bad);
+                a = fma(-ms, M[j][c], ps * a);
+            } else if (c == r) {
+                a = ps * a;  // the diagonal of a finished row scales with its row
+            }
+        }
+    }
+    // lane (r, 6) divides by the diagonal (r, r) of its row, held in the same warp
+    const double d = __shfl_sync(0xffffffffu, a, act ? (l / 7) * 7 + r : 0);
+    bool inf = false;
+    if (act && c == 6) {
+        const double xr = (d > 0x1p-1000 && d < 0x1p1000) ? div_pivot(a, d) : a / d;
+        inf = !isfinite(xr);
+        x[r] = xr;
+    }
+    // out of range anywhere: neither the decision nor x can be trusted (a subnormal
+    // pivot, say, scales to zero and makes the next pivot zero)
+    if (!pair_bar_or(bar_id + 1, bad || (pd && inf))) return pd;  // also publishes x
+    // rare: redo with IEEE divisions by the first warp; the second waits at the barrier
+    bool fail = false;
+    if (w == 0) {
+        double col[6];
+#pragma unroll
+        for (int i = 0; i < 6; ++i) col[i] = l < 7 ? entry(i, l) : 0.0;
+        fail = !warp_gj6_f64_ieee(col);
+        if (l == 6 && !fail)
+#pragma unroll
+            for (int i = 0; i < 6; ++i) x[i] = col[i];
+    }
+    return !pair_bar_or(bar_id + 1, fail && l == 0);
 }
 
 }  // namespace kf

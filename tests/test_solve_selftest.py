@@ -56,10 +56,10 @@ def _icp_like_systems(rng, n):
 
 
 def test_fp64_solve_against_numpy():
-    """The precision form's FP64 warp solve (Gauss-Jordan with Newton-refined pivot
-    reciprocals) against numpy's FP64 Cholesky solve: the same positive-definite
-    decision away from the boundary, and solutions within 1e-12 relative (scaled by the
-    system's condition number) where it solves."""
+    """The precision form's FP64 solve (fraction-free Gauss-Jordan by a warp pair, one
+    series-refined reciprocal per row) against numpy's FP64 solve: the same
+    positive-definite decision away from the boundary, and solutions within 1e-12
+    relative (scaled by the system's condition number) where it solves."""
     rng = np.random.default_rng(7)
     n = 4096
     A, b = _icp_like_systems(rng, n)
@@ -83,3 +83,39 @@ def test_fp64_solve_against_numpy():
             assert err <= 1e-12 / ratio + 1e-14, (k, err, ratio)
     assert n_pd > 0.5 * n
     assert (ok == 0).sum() > 0.05 * n
+
+
+def test_fp64_solve_far_from_unit_scale():
+    """Systems scaled by powers of two (exact, the solution unchanged).  Near 2^-1010 and
+    2^1012 the final divisions leave the refined reciprocal's range and fall back to
+    IEEE division; with subnormal entries (2^-1060) the pivots are subnormal and the
+    whole system is solved again by the IEEE Gauss-Jordan fallback.  The systems are
+    well-conditioned and positive definite, so all three must match numpy's solve of the
+    same system at unit scale."""
+    rng = np.random.default_rng(11)
+    n = 96
+    A = np.zeros((n, 6, 6))
+    for k in range(n):
+        q = rng.normal(size=(6, 6))
+        A[k] = q @ q.T + 6.0 * np.eye(6)
+    b = rng.normal(size=(n, 6))
+    ref = np.linalg.solve(A, b[..., None])[..., 0]
+    scales = np.array([2.0 ** -1010, 2.0 ** -1060, 2.0 ** 1012])
+    for sc in scales:
+        As = A * sc
+        bs = b * sc
+        tiny = sc < 2.0 ** -1022
+        if tiny:
+            # the subnormal inputs are rounded: the reference is the rounded system
+            ref_k = np.linalg.solve(As / sc, (bs / sc)[..., None])[..., 0]
+        else:
+            ref_k = ref
+        x = np.zeros((n, 6))
+        ok = np.zeros(n, np.int32)
+        lib = _lib.load()
+        st = lib.kf_selftest_solve6(As.ctypes.data, bs.ctypes.data, x.ctypes.data, ok.ctypes.data, n)
+        assert st == _lib.KF_OK
+        assert ok.all(), sc
+        err = np.abs(x - ref_k).max() / np.abs(ref_k).max()
+        # subnormal arithmetic keeps only an absolute 2^-1074 (~2^-17 of these entries)
+        assert err <= (1e-3 if tiny else 1e-12), (sc, err)
