@@ -682,13 +682,14 @@ __device__ __forceinline__ void solve_body(const float* __restrict__ partials, i
 // atomic addition (integer addition commutes, so the result does not depend on the
 // order the blocks arrive in).  The last block to finish (a ticket) reads and clears
 // the accumulators, carries the digits into one integer per sum, converts it to FP64
-// and solves (finish_precise_warp, MODE 0) or writes the float sums (MODE 1).  Nothing
+// and solves (finish_precise_pair, MODE 0) or writes the float sums (MODE 1).  Nothing
 // waits for a second pass over the partials.  Every block value below 2^79 in magnitude
 // is held exactly (to 2^-48), and the digit accumulators stay below 2^63 for fewer than
 // 2^31 blocks, so their sum is exact; a non-finite or larger block value marks its sum
-// NaN, as the float sum would have gone infinite or NaN.  The accumulators of a sum are
-// spread over kFixReplicas copies (block b adds to copy b % kFixReplicas), one 128-byte
-// line per digit and copy, so that few atomic additions queue on any one line.
+// NaN, as the float sum would have gone infinite or NaN.  The accumulators are spread
+// over kFixReplicas copies (block b adds to copy b % kFixReplicas), so that few atomic
+// additions queue on any one word; within a copy the 112 digits are consecutive, so a
+// block's additions and the last block's reads are whole-line (coalesced) accesses.
 namespace fix {
 
 // f * 2^48 truncated toward zero as a 128-bit two's-complement integer (hi, lo); false
@@ -719,63 +720,56 @@ __device__ __forceinline__ bool to_fixed(float f, unsigned long long& hi, unsign
 }
 
 constexpr int kFixReplicas = 16;
+constexpr int kDigits = kIcpVals * 4;  // words per copy: 7 lines of 128 bytes
 
-// the accumulator of digit d of sum k in copy r
-__device__ __forceinline__ unsigned long long* digit(long long* acc, int k, int d, int r)
+// copy r of the accumulators: kDigits consecutive words, digit d of sum k at k * 4 + d
+__device__ __forceinline__ unsigned long long* copy_of(long long* acc, int r)
 {
-    return reinterpret_cast<unsigned long long*>(acc) + ((size_t)((k * 4 + d) * kFixReplicas + r) * 16);
+    return reinterpret_cast<unsigned long long*>(acc) + (size_t)r * kDigits;
 }
 
-// adds hi + lo (a compensated pair) to sum k's accumulator (replica r); flags sum k if
-// either part cannot be represented
-__device__ __forceinline__ void accumulate(long long* acc, unsigned* bad, int k, int r, float h, float l)
+// the four digits of hi + lo (a compensated pair): three unsigned 32-bit digits and the
+// signed top digit; false (digits zero) if either part cannot be represented
+__device__ __forceinline__ bool digits_of(float h, float l, unsigned long long (&dg)[4])
 {
     unsigned long long h1, l1, h2, l2;
     const bool ok = to_fixed(h, h1, l1) & to_fixed(l, h2, l2);
-    if (!ok) {
-        atomicOr(bad, 1u << k);
-        return;
-    }
     const unsigned long long lo = l1 + l2;
     const unsigned long long hi = h1 + h2 + (lo < l1 ? 1ull : 0ull);
-    atomicAdd(digit(acc, k, 0, r), lo & 0xffffffffull);
-    atomicAdd(digit(acc, k, 1, r), lo >> 32);
-    atomicAdd(digit(acc, k, 2, r), hi & 0xffffffffull);
-    atomicAdd(digit(acc, k, 3, r), (unsigned long long)((long long)hi >> 32));  // the signed top digit
+    dg[0] = ok ? lo & 0xffffffffull : 0ull;
+    dg[1] = ok ? lo >> 32 : 0ull;
+    dg[2] = ok ? hi & 0xffffffffull : 0ull;
+    dg[3] = ok ? (unsigned long long)((long long)hi >> 32) : 0ull;
+    return ok;
 }
 
-// The last block's read-out, all threads of the block: each digit's replicas are read
-// (every load issued before any is used), added, and cleared; digits[k * 4 + d] (shared)
-// receives digit d of sum k, and *bad_out (shared) the flags of the sums that could not
-// be accumulated (read and cleared in the same round of loads).
+// The last block's read-out, all threads of the block: thread t < kDigits reads word t
+// of every copy (each load instruction covers 32 consecutive words, and all are issued
+// before any is used), adds them and clears them; digits[t] (shared) receives the sum,
+// and *bad_out (shared) the flags of the sums that could not be accumulated (read and
+// cleared in the same round of loads).
 __device__ __forceinline__ void gather_digits(long long* acc, long long* digits, unsigned* bad_flags,
                                               unsigned* bad_out)
 {
-    static_assert(kIcpVals * 4 * 2 < kExactWarps * 32 && kFixReplicas % 2 == 0, "two threads per digit");
-    const int t = threadIdx.x, D = t >> 1, half = t & 1;
-    constexpr int kPer = kFixReplicas / 2;
-    long long v = 0;
+    static_assert(kDigits < kExactWarps * 32, "one thread per digit and one for the flags");
+    const int t = threadIdx.x;
     if (t == kExactWarps * 32 - 1) {
         // every other block's atomicOr on the flags came before its ticket
         *bad_out = __ldcg(bad_flags);
         __stcg(bad_flags, 0u);
     }
-    if (D < kIcpVals * 4) {
-        unsigned long long* w[kPer];
-        unsigned long long x[kPer];
+    if (t < kDigits) {
+        unsigned long long x[kFixReplicas];
 #pragma unroll
-        for (int i = 0; i < kPer; ++i) {
-            w[i] = digit(acc, D >> 2, D & 3, half * kPer + i);
-            x[i] = __ldcg(w[i]);
-        }
+        for (int i = 0; i < kFixReplicas; ++i) x[i] = __ldcg(copy_of(acc, i) + t);
+        long long v = 0;
 #pragma unroll
-        for (int i = 0; i < kPer; ++i) {
+        for (int i = 0; i < kFixReplicas; ++i) {
             v += (long long)x[i];
-            __stcg(w[i], 0ull);
+            __stcg(copy_of(acc, i) + t, 0ull);
         }
+        digits[t] = v;
     }
-    v += __shfl_xor_sync(0xffffffffu, v, 1);
-    if (D < kIcpVals * 4 && half == 0) digits[D] = v;
     __syncthreads();
 }
 
@@ -865,6 +859,7 @@ __global__ void __launch_bounds__(kExactWarps * 32, 4) icp_precise_kernel(
     if (!prefetch) load_pair(grp * 64 + lane, n, vmap, nmap, v, nn);
     __shared__ float sF[16], sT[16];
     __shared__ float wsum[kExactWarps][kIcpVals];
+    __shared__ unsigned long long sdig[fix::kDigits];
     __shared__ int is_last;
     if (threadIdx.x < 16) {
         sF[threadIdx.x] = Fsrc[threadIdx.x];
@@ -898,7 +893,15 @@ __global__ void __launch_bounds__(kExactWarps * 32, 4) icp_precise_kernel(
             h = sum;
             l += e;
         }
-        fix::accumulate(fixacc, &st->fix_bad, k, blockIdx.x % fix::kFixReplicas, h, l);
+        unsigned long long dg[4];
+        if (!fix::digits_of(h, l, dg)) atomicOr(&st->fix_bad, 1u << k);
+#pragma unroll
+        for (int d = 0; d < 4; ++d) sdig[k * 4 + d] = dg[d];
+    }
+    __syncthreads();
+    // one atomic addition per digit, 32 consecutive words per instruction
+    if (threadIdx.x < fix::kDigits) {
+        atomicAdd(fix::copy_of(fixacc, blockIdx.x % fix::kFixReplicas) + threadIdx.x, sdig[threadIdx.x]);
         __threadfence();
     }
     __syncthreads();
@@ -978,7 +981,7 @@ int icp_groups(int H, int W) { return (H * W + 63) / 64; }
 
 void icp_prepare(int H, int W) { ensure_solve_smem(icp_groups(H, W)); }
 
-size_t icp_fixacc_words() { return (size_t)kIcpVals * 4 * fix::kFixReplicas * 16; }
+size_t icp_fixacc_words() { return (size_t)fix::kDigits * fix::kFixReplicas; }
 
 size_t icp_scratch_floats(int H, int W)
 {

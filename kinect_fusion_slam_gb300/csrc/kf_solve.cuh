@@ -348,18 +348,15 @@ __device__ __forceinline__ bool pair_bar_or(int id, bool v)
 // v * 2^(1023 - e), e the exponent field of a normal pivot, by integer arithmetic on
 // v's exponent field (exact where the result is normal).  Zero where v is zero or
 // subnormal or the result would be subnormal (a term below 2^-1022 of the pivot row's
-// scale); `over` is set where the result would overflow or v is not finite.
+// scale); `over` is set where the result would overflow or v is not finite.  No branch.
 __device__ __forceinline__ double scale_by_pivot(double v, int e, bool& over)
 {
     const int hi = __double2hiint(v), lo = __double2loint(v);
     const int ev = (hi >> 20) & 0x7ff;
     const int en = ev - e + 1023;
-    if (ev == 0x7ff || en > 2046) {
-        over = true;
-        return v;
-    }
-    if (ev == 0 || en < 1) return 0.0;
-    return __hiloint2double((hi & 0x800fffff) | (en << 20), lo);
+    over = over || ev == 0x7ff || en > 2046;
+    const double sc = __hiloint2double((hi & 0x800fffff) | ((en & 0x7ff) << 20), lo);
+    return (ev == 0 || en < 1) ? 0.0 : sc;
 }
 
 // The precision form's 6x6 solve A x = b in FP64 by a pair of warps (the 64 threads
@@ -401,14 +398,13 @@ __device__ __forceinline__ bool pair_gj6_f64(const Entry& entry, int t, double (
         pd = pd && p > 0.0;
         bad = bad || ep == 0 || ep == 0x7ff;
         const double ps = scale_by_pivot(p, ep, bad);  // in [1, 2)
-        if (act && r != j) {
-            if (c > j) {
-                const double ms = scale_by_pivot(M[r][j], ep, bad);
-                a = fma(-ms, M[j][c], ps * a);
-            } else if (c == r) {
-                a = ps * a;  // the diagonal of a finished row scales with its row
-            }
-        }
+        // rows i != j: a <- p' a - m' q on the live columns c > j, a <- p' a elsewhere
+        // (on the diagonal of a finished row, which scales with its row; the other
+        // entries there are dead); row j stays.  Two FP64 operations in every lane,
+        // without divergence.
+        const double q = M[j][c];
+        const double ms = (r != j && c > j) ? scale_by_pivot(M[r][j], ep, bad) : 0.0;
+        a = fma(-ms, q, (r == j ? 1.0 : ps) * a);
     }
     // lane (r, 6) divides by the diagonal (r, r) of its row, held in the same warp
     const double d = __shfl_sync(0xffffffffu, a, act ? (l / 7) * 7 + r : 0);
