@@ -33,6 +33,10 @@ struct IcpParams {
     int fail_mode;        // 0 reference (raw b), 1 identity
     int precise;          // compensated sums + FP64 solve
     int reference_order;  // sums in the reference's order (bit-identical to it)
+    // the precision form's association gates in the form it evaluates them: dist^2
+    // (negative: nothing passes) and cos(angle)
+    float dist2;
+    float cos_angle;
 };
 
 // Per-handle device state, updated by the kernels so that a whole frame runs without

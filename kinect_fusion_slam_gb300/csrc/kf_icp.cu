@@ -10,6 +10,7 @@
 // the system like cv::Cholesky, forms the small-angle increment and updates the pose
 // in device memory.  The reduction order differs from the reference's 64-wide tree +
 // serial host sum, so the sums agree to float rounding, not bit for bit.
+#include <cmath>
 #include <cstddef>
 
 #include "kf_kernels.h"
@@ -178,6 +179,92 @@ __device__ __forceinline__ void associate_pair(int i0, int n, const float4* __re
     float4 v[2], nn[2];
     load_pair(i0, n, vmap, nmap, v, nn);
     associate_pair_from(v, nn, pv, pn, cam, F, T, dist_th, ang_th, ok, a, b, j);
+}
+
+// The precision form's association: the gates, matched pixel, row a and residual b of
+// assoc_project + assoc_finish (sensor_pose_estimation.cu:20-131), in FP32 with the
+// arithmetic arranged for fewer instructions -- products fused into FMAs, the
+// perspective division by one approximate reciprocal (q = p.x * rcp(p.z), |error| of a
+// few ulps), round(q) as floor(q + 0.5) (the same for the q >= 0 that can pass), the
+// distance gate on the squared distance, and the angle gate acos(<Rn/|Rn|, m/|m|>) <= th
+// as a comparison of <Rn, m>^2 with cos^2(th) |Rn|^2 |m|^2 (with the sign of <Rn, m>)
+// that needs neither normalisation nor acos.  The terms are the same functions of the
+// same inputs; a pixel whose projection lies within a few ulps of a pixel boundary, or
+// whose distance or angle lies within an ulp of its gate, may be decided differently
+// from the plain form (a few dozen pixels of 307 200 at 640x480).
+__device__ __forceinline__ bool lean_project(float4 v, const Camera& cam, const float* F, const float* T, float3& g,
+                                             int& j)
+{
+    if (!(v.z != 0 && v.w != 0)) return false;
+    const float cx = fmaf(F[0], v.x, fmaf(F[1], v.y, fmaf(F[2], v.z, F[3])));
+    const float cy = fmaf(F[4], v.x, fmaf(F[5], v.y, fmaf(F[6], v.z, F[7])));
+    const float cz = fmaf(F[8], v.x, fmaf(F[9], v.y, fmaf(F[10], v.z, F[11])));
+    const float* K = cam.K;
+    const float px = fmaf(K[0], cx, fmaf(K[1], cy, K[2] * cz));
+    const float py = fmaf(K[3], cx, fmaf(K[4], cy, K[5] * cz));
+    const float pz = fmaf(K[6], cx, fmaf(K[7], cy, K[8] * cz));
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(pz));
+    // NaN converts to 0 and +-inf saturate: all outside the image, like the reference
+    const int u = (int)floorf(fmaf(px, r, 0.5f));
+    const int vv = (int)floorf(fmaf(py, r, 0.5f));
+    if (!(u > 0 && u <= cam.W && vv > 0 && vv <= cam.H)) return false;
+    g.x = fmaf(T[0], v.x, fmaf(T[1], v.y, fmaf(T[2], v.z, T[3])));
+    g.y = fmaf(T[4], v.x, fmaf(T[5], v.y, fmaf(T[6], v.z, T[7])));
+    g.z = fmaf(T[8], v.x, fmaf(T[9], v.y, fmaf(T[10], v.z, T[11])));
+    j = (vv - 1) * cam.W + (u - 1);
+    return true;
+}
+
+__device__ __forceinline__ bool lean_finish(float3 g, float4 n, float4 q, float4 m, const float* T, float dist2,
+                                            float cos_th, float (&a)[6], float& b)
+{
+    const float dx = g.x - q.x, dy = g.y - q.y, dz = g.z - q.z;
+    const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+    if (!(d2 <= dist2)) return false;
+    const float rx = fmaf(T[0], n.x, fmaf(T[1], n.y, T[2] * n.z));
+    const float ry = fmaf(T[4], n.x, fmaf(T[5], n.y, T[6] * n.z));
+    const float rz = fmaf(T[8], n.x, fmaf(T[9], n.y, T[10] * n.z));
+    const float ct = fmaf(rx, m.x, fmaf(ry, m.y, rz * m.z));
+    const float nn = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
+    const float mm = fmaf(m.x, m.x, fmaf(m.y, m.y, m.z * m.z));
+    const float lhs = ct * ct, rhs = (cos_th * cos_th) * (nn * mm);
+    // a zero normal is NaN in the reference and rejects; so does NaN here
+    const bool ang = cos_th >= 0.f ? (ct > 0.f && lhs >= rhs) : (ct >= 0.f || lhs <= rhs);
+    if (!(nn > 0.f && mm > 0.f && ang)) return false;
+    a[0] = fmaf(g.z, m.y, -(g.y * m.z));
+    a[1] = fmaf(g.x, m.z, -(g.z * m.x));
+    a[2] = fmaf(g.y, m.x, -(g.x * m.y));
+    a[3] = m.x;
+    a[4] = m.y;
+    a[5] = m.z;
+    b = -fmaf(m.x, dx, fmaf(m.y, dy, m.z * dz));  // m . (q - g)
+    return true;
+}
+
+// associate_pair_from with the precision form's arithmetic: both projections, then both
+// gathers, then both gates
+__device__ __forceinline__ void lean_pair(const float4 (&v)[2], const float4 (&nn)[2], const float4* __restrict__ pv,
+                                          const float4* __restrict__ pn, const Camera& cam, const float* F,
+                                          const float* T, float dist2, float cos_th, bool (&ok)[2], float (&a)[2][6],
+                                          float (&b)[2], int (&j)[2])
+{
+    const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+    float3 g[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        j[h] = -1;
+        ok[h] = lean_project(v[h], cam, F, T, g[h], j[h]);
+    }
+    float4 q[2], m[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        q[h] = ok[h] ? pv[j[h]] : zero;
+        m[h] = ok[h] ? pn[j[h]] : zero;
+    }
+#pragma unroll
+    for (int h = 0; h < 2; ++h)
+        if (ok[h]) ok[h] = lean_finish(g[h], nn[h], q[h], m[h], T, dist2, cos_th, a[h], b[h]);
 }
 
 // Deterministic block reduction: butterfly shuffles within each warp, then warp
@@ -420,6 +507,18 @@ __device__ __forceinline__ void add_terms(float (&v)[kIcpVals], const float (&a)
     for (int r = 0; r < 6; ++r)
 #pragma unroll
         for (int s = r; s < 6; ++s) v[tri(r, s)] = v[tri(r, s)] + a[r] * a[s];
+    v[kIcpVals - 1] = v[kIcpVals - 1] + 1.f;
+}
+
+// add_terms with each product fused into its addition (the precision form)
+__device__ __forceinline__ void add_terms_fused(float (&v)[kIcpVals], const float (&a)[6], float b)
+{
+#pragma unroll
+    for (int r = 0; r < 6; ++r) v[r] = fmaf(a[r], b, v[r]);
+#pragma unroll
+    for (int r = 0; r < 6; ++r)
+#pragma unroll
+        for (int s = r; s < 6; ++s) v[tri(r, s)] = fmaf(a[r], a[s], v[tri(r, s)]);
     v[kIcpVals - 1] = v[kIcpVals - 1] + 1.f;
 }
 
@@ -873,13 +972,13 @@ __global__ void __launch_bounds__(kExactWarps * 32, 4) icp_precise_kernel(
         bool ok[2];
         float a[2][6], b[2];
         int j[2];
-        associate_pair_from(v, nn, pv, pn, cam, sF, sT, prm.dist, prm.angle_deg, ok, a, b, j);
+        lean_pair(v, nn, pv, pn, cam, sF, sT, prm.dist2, prm.cos_angle, ok, a, b, j);
         if (MODE == 1 && pair) {
             if (grp * 64 + lane < n) pair[grp * 64 + lane] = ok[0] ? j[0] : -1;
             if (grp * 64 + 32 + lane < n) pair[grp * 64 + 32 + lane] = ok[1] ? j[1] : -1;
         }
-        if (ok[0]) add_terms(vals, a[0], b[0]);
-        if (ok[1]) add_terms(vals, a[1], b[1]);
+        if (ok[0]) add_terms_fused(vals, a[0], b[0]);
+        if (ok[1]) add_terms_fused(vals, a[1], b[1]);
     }
     const float vs = warp_sum_transposed(vals);  // the whole warp: also where grp >= ngroups
     if (lane < kIcpVals) wsum[warp][lane] = vs;
@@ -991,6 +1090,15 @@ size_t icp_scratch_floats(int H, int W)
 }
 
 namespace {
+// the precision form's gate constants (lean_finish)
+IcpParams lean_params(const IcpParams& prm)
+{
+    IcpParams q = prm;
+    q.dist2 = prm.dist >= 0.f ? prm.dist * prm.dist : -1.f;
+    q.cos_angle = prm.angle_deg < 0.f ? 2.f : (float)std::cos((double)prm.angle_deg * (3.14159265358979323846 / 180.0));
+    return q;
+}
+
 int exact_blocks(int H, int W)
 {
     const int g = icp_groups(H, W);
@@ -1013,8 +1121,8 @@ void launch_icp_iteration(const float4* vmap, const float4* nmap, const float4* 
     } else if (prm.precise) {
         const int ng = icp_groups(cam.H, cam.W);
         launch_pdl(icp_precise_kernel<0>, dim3(exact_blocks(cam.H, cam.W)), dim3(kExactWarps * 32), 0, s, vmap, nmap,
-                   pv, pn, cam, prm, state_F(st), state_T(st), st, fixacc, ng, after_pass ? 1 : 0, (int32_t*)nullptr,
-                   (float*)nullptr);
+                   pv, pn, cam, lean_params(prm), state_F(st), state_T(st), st, fixacc, ng, after_pass ? 1 : 0,
+                   (int32_t*)nullptr, (float*)nullptr);
     } else
         icp_kernel<0><<<blocks, kIcpBlock, 0, s>>>(vmap, nmap, pv, pn, cam, prm, st, state_F(st), state_T(st),
                                                    partials, nullptr, nullptr);
@@ -1036,7 +1144,7 @@ void launch_icp_associate(const float4* vmap, const float4* nmap, const float4* 
     } else if (prm.precise) {
         const int ng = icp_groups(cam.H, cam.W);
         launch_pdl(icp_precise_kernel<1>, dim3(exact_blocks(cam.H, cam.W)), dim3(kExactWarps * 32), 0, s, vmap, nmap,
-                   pv, pn, cam, prm, F, T, st, fixacc, ng, 0, pair, sums_out);
+                   pv, pn, cam, lean_params(prm), F, T, st, fixacc, ng, 0, pair, sums_out);
     } else
         icp_kernel<1><<<blocks, kIcpBlock, 0, s>>>(vmap, nmap, pv, pn, cam, prm, st, F, T, partials,
                                                           sums_out, pair);
