@@ -17,6 +17,7 @@ namespace kf {
 namespace {
 
 struct VolF32 {
+    static constexpr bool kLean = false;  // the reference's arithmetic, operation for operation
     float* t;
     float* w;
     __device__ __forceinline__ void load(int i, float& tv, float& wv) const
@@ -32,6 +33,10 @@ struct VolF32 {
 };
 
 struct VolF16 {
+    // the FP16 form's integration arithmetic (integrate_at): the voxel's pixel as in the
+    // reference (IEEE quotients), its distance and value by approximate square root and
+    // reciprocals, which the 11-bit storage cannot tell from the IEEE operations
+    static constexpr bool kLean = true;
     __half2* p;
     __device__ __forceinline__ void load(int i, float& tv, float& wv) const
     {
@@ -421,6 +426,7 @@ __device__ __forceinline__ void integrate_at(const Vol& vol, const float2* __res
     // outside exactly and needs neither division (NaN compares false and falls through)
     const float ulo = 0.5f - 1e-3f, uhi = (float)W + 0.5f + 1e-3f * (float)W;
     const float vlo = 0.5f - 1e-3f, vhi = (float)H + 0.5f + 1e-3f * (float)H;
+    const float inv_trunc = 1.f / g.trunc;
     for (int z = z0; z < z1; ++z, lin += zstride) {
         if (may_skip && rbase + z >= p.skip_from) continue;
         const float vcz = centre(z, g.sz, g.vd);
@@ -446,12 +452,17 @@ __device__ __forceinline__ void integrate_at(const Vol& vol, const float2* __res
         if (u < 1 || u > W || v < 1 || v > H) continue;
         const float2 e = __ldg(tab + (v - 1) * W + (u - 1));
         if (isnan(e.x)) continue;
-        const float tm = sqrtf(m0 + tdz * tdz);
+        float tm;
+        if (Vol::kLean)
+            asm("sqrt.approx.f32 %0, %1;" : "=f"(tm) : "f"(m0 + tdz * tdz));
+        else
+            tm = sqrtf(m0 + tdz * tdz);
         const float frk = e.x - e.y * tm;
         const bool ahead = frk > 0 && frk <= g.sdf_max;
         const bool behind = frk <= 0 && frk >= g.sdf_min;
         if (!ahead && !behind) continue;
-        const float f = ahead ? fminf(1.f, frk / g.trunc) : fmaxf(-1.f, frk / g.trunc);
+        const float fq = Vol::kLean ? frk * inv_trunc : frk / g.trunc;
+        const float f = ahead ? fminf(1.f, fq) : fmaxf(-1.f, fq);
         if (FIRST) {
             vol.store(lin, f, 1.0f);
         } else {
@@ -459,7 +470,13 @@ __device__ __forceinline__ void integrate_at(const Vol& vol, const float2* __res
             vol.load(lin, t, w);
             if (isnan(t)) t = 0.0f;
             if (isnan(w)) w = 0.0f;
-            vol.store(lin, (w * t + 1.0f * f) / (w + 1.0f), w + 1.0f);
+            if (Vol::kLean) {
+                float rw;
+                asm("rcp.approx.f32 %0, %1;" : "=f"(rw) : "f"(w + 1.0f));
+                vol.store(lin, fmaf(w, t, f) * rw, w + 1.0f);
+            } else {
+                vol.store(lin, (w * t + 1.0f * f) / (w + 1.0f), w + 1.0f);
+            }
         }
     }
 }
