@@ -35,12 +35,25 @@ __device__ __forceinline__ void vertex_body(int i, const uint16_t* __restrict__ 
                                             float dmin, float dmax, State* st, int init_icp, int normals)
 {
     const int H = cam.H, W = cam.W;
-    if (init_icp && i == 0) {
-        // frame start of Estimate_Sensor_Pose (sensor_pose_estimation.cu:255-259, 343)
-        inv4(st->T, st->Tprev_inv);
-        mat4(st->Tprev_inv, st->T, st->F);
-        for (int k = 0; k < 16; ++k) st->Td[k] = (double)st->T[k];
-        st->iter = 0;
+    if (init_icp && i < 32) {
+        // Frame start of Estimate_Sensor_Pose (sensor_pose_estimation.cu:255-259, 343),
+        // by the first warp: T_prev^-1 = inv4(T), F = mat4(T_prev^-1, T).  The previous
+        // frame's integration inverted the same pose when T has not changed since, so
+        // its inverse is copied; otherwise the warp inverts T.
+        const int lane = i;
+        const bool same = __all_sync(0xffffffffu, lane >= 16 || __float_as_uint(st->T[lane]) ==
+                                                                    __float_as_uint(st->Tinv_src[lane]));
+        if (same) {
+            if (lane < 16) st->Tprev_inv[lane] = st->Tinv[lane];
+        } else {
+            inv4_warp(st->T, st->Tprev_inv);
+        }
+        __syncwarp();
+        if (lane < 16) {
+            st->F[lane] = mat4_at(st->Tprev_inv, st->T, lane);
+            st->Td[lane] = (double)st->T[lane];
+        }
+        if (lane == 0) st->iter = 0;
     }
     if (i >= H * W) return;
     const int row = i / W, col = i % W;
@@ -100,7 +113,7 @@ __global__ void __launch_bounds__(256) vertex_batch_kernel(const SceneDev* __res
     const SceneDev& d = scenes[blockIdx.y];
     const Camera& cam = d.cam[level];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= cam.H * cam.W && !(init_icp && i == 0)) return;
+    if (i >= cam.H * cam.W && !(init_icp && i < 32)) return;  // the first warp sets up the ICP
     if (level == 0)
         vertex_body<true>(i, d.raw, d.depth[0], d.vmap[0], d.nmap[0], cam, d.dmin, d.dmax, d.st, init_icp, 1);
     else

@@ -47,6 +47,7 @@ struct State {
     float Tprev_inv[16];  // inverse of the pose at the start of the frame's ICP
     float F[16];          // Tprev_inv * T, the frame-to-frame transform of the iteration
     float Tinv[16];       // inverse of the pose used by integration
+    float Tinv_src[16];   // the pose Tinv was computed from
     float axis[3];        // "in front of the camera" direction (projective_tsdf.cu:57-71)
     float c_flip;         // ray-cast normal flip threshold (voxel_traversal.cu:361-369)
     double Td[16];        // FP64 pose (precise solve mode)

@@ -91,6 +91,77 @@ KF_HD bool inv4(const float* src, float* out)
     return true;
 }
 
+#if defined(__CUDACC__)
+// inv4 by one warp (all 32 lanes call), bit-identical to inv4: lane l holds entry
+// (r, c) = (l >> 3, l & 7) of [a | b] (c < 4: a; c >= 4: b, the identity on entry), and
+// every operation of inv4 on an entry is done by that entry's lane, in inv4's order:
+// the pivot search runs the same compares in every lane, rows are swapped by shuffles,
+// each elimination step is one product and one sum per lane, and the back substitution
+// runs row by row with the four columns in parallel.  Writes out[0..15] from the lanes
+// holding b (or zeros, and returns false, where inv4 would).
+__device__ __forceinline__ bool inv4_warp(const float* src, float* out)
+{
+    const unsigned full = 0xffffffffu;
+    const int l = threadIdx.x & 31, r = l >> 3, c = l & 7;
+    float v = c < 4 ? src[r * 4 + c] : (c - 4 == r ? 1.f : 0.f);
+    const float eps = FLT_EPSILON * 10;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        float col[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) col[j] = __shfl_sync(full, v, j * 8 + i);
+        int p = i;
+        float best = col[i];
+#pragma unroll
+        for (int j = i + 1; j < 4; ++j)
+            if (fabsf(col[j]) > fabsf(best)) {
+                p = j;
+                best = col[j];
+            }
+        if (fabsf(best) < eps) {  // the same in every lane
+            if (l < 16) out[l] = 0.f;
+            return false;
+        }
+        // rows i and p trade their a entries from column i on and all their b entries
+        const int from = r == i ? p : (r == p ? i : r);
+        const float other = __shfl_sync(full, v, from * 8 + c);
+        if (from != r && (c >= 4 || c >= i)) v = other;
+        const float d = -1 / __shfl_sync(full, v, i * 8 + i);
+        const float aji = __shfl_sync(full, v, r * 8 + i);
+        const float aic = __shfl_sync(full, v, i * 8 + c);
+        if (r > i && (c >= 4 || c > i)) {
+            const float alpha = aji * d;
+            v += alpha * aic;
+        }
+    }
+#pragma unroll
+    for (int i = 3; i >= 0; --i) {
+        float s = v;
+#pragma unroll
+        for (int k = i + 1; k < 4; ++k) {
+            const float aik = __shfl_sync(full, v, i * 8 + k);
+            const float bkj = __shfl_sync(full, v, k * 8 + c);
+            s -= aik * bkj;
+        }
+        const float aii = __shfl_sync(full, v, i * 8 + i);
+        if (r == i && c >= 4) v = s / aii;
+    }
+    if (c >= 4) out[r * 4 + (c - 4)] = v;
+    return true;
+}
+
+// entry (r, c) = (k >> 2, k & 3) of mat4(a, b)
+__device__ __forceinline__ float mat4_at(const float* a, const float* b, int k)
+{
+    const int i = k >> 2, j = k & 3;
+    double s = (double)a[i * 4 + 0] * b[j];
+    s += (double)a[i * 4 + 1] * b[4 + j];
+    s += (double)a[i * 4 + 2] * b[8 + j];
+    s += (double)a[i * 4 + 3] * b[12 + j];
+    return (float)s;
+}
+#endif
+
 // out = a * b (out may alias a or b)
 KF_HD void mat4(const float* a, const float* b, float* out)
 {

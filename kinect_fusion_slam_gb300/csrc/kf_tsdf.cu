@@ -70,8 +70,8 @@ struct ViewF16 {
 
 // Per pixel (u, v) (1-based): the quantities of projective_tsdf.cu:39-95 that depend
 // only on the pixel and the pose.  tab = (predicted_depth or NaN where the depth is
-// 0, 1 / |ray direction|).  Thread 0 also stores T^-1 (cv::Mat::inv, :149) and the
-// in-front axis (:57-71).
+// 0, 1 / |ray direction|).  Thread 0 also stores the in-front axis (:57-71); the warp
+// of tile 0 stores T^-1 (cv::Mat::inv, :149; integrate_prep_tile).
 __device__ __forceinline__ void integrate_prep_at(int i, const float* __restrict__ depth, float2* __restrict__ tab,
                                                   const Camera& cam, State* st)
 {
@@ -81,7 +81,6 @@ __device__ __forceinline__ void integrate_prep_at(int i, const float* __restrict
 #pragma unroll
     for (int k = 0; k < 16; ++k) T[k] = st->T[k];
     if (i == 0) {
-        inv4(T, st->Tinv);
         const float3 ca = mul3(Ki, make_float3(K[5], K[2], 1.f));
         const float3 cb = make_float3(2 * (Ki[0] * K[5] + Ki[1] * K[2] + Ki[2] * 1.f),
                                       2 * (Ki[3] * K[5] + Ki[4] * K[2] + Ki[5] * 1.f),
@@ -126,6 +125,12 @@ __device__ __forceinline__ void integrate_prep_tile(int tile, int lane, const fl
     const int H = cam.H, W = cam.W;
     const int ntx = bound_tiles_x(W);
     const int x0 = (tile % ntx) * kBoundTile, y0 = (tile / ntx) * kBoundTile;
+    if (tile == 0) {
+        // T^-1 for integration, and the pose it inverts (the next frame's ICP reuses
+        // the inverse while the pose is unchanged)
+        inv4_warp(st->T, st->Tinv);
+        if (lane < 16) st->Tinv_src[lane] = st->T[lane];
+    }
     float lo = INFINITY, hi = -INFINITY;
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
