@@ -605,7 +605,6 @@ __device__ __forceinline__ void trace(const View& vol, float X, float Y, float D
     int ix = (int)floorf(((s.x - lo.x) / box.x) * L) + 1;
     int iy = (int)floorf(((s.y - lo.y) / box.y) * Wd) + 1;
     int iz = (int)floorf(((s.z - lo.z) / box.z) * Hz) + 1;
-    int XY = 0, XZ = 0, YX = 0, YZ = 0, ZX = 0, ZY = 0;
     if (ix == L + 1) ix = ix - 1;
     if (iy == Wd + 1) iy = iy - 1;
     if (iz == Hz + 1) iz = iz - 1;
@@ -646,93 +645,121 @@ __device__ __forceinline__ void trace(const View& vol, float X, float Y, float D
         return (unsigned)(a - 1) < (unsigned)(L - 2) && (unsigned)(b - 1) < (unsigned)(Wd - 2) &&
                (unsigned)(c - 1) < (unsigned)(Hz - 2);
     };
-    // The Amanatides-Woo step (:384-417) without branches: the same three comparisons
-    // pick the axis; selects apply the step.
-    auto pick = [](float3 t, bool& bx, bool& by, bool& bz) {
-        const bool xy = t.x < t.y, xz = t.x < t.z, yz = t.y < t.z;
-        bx = xy && xz;
-        by = !xy && yz;
-        bz = !(bx || by);
-    };
+    // The walk visits positions 0, 1, 2, ... until the first one outside the loop bounds
+    // (:203-205).  The start is tested once; after it every index moves in one fixed
+    // direction, so each axis can leave the bounds only on one side, and a position is
+    // inside iff the steps each axis has left before that side, r = (n - 2) - i going up
+    // or i - 1 going down, are all >= 0 -- one OR and one sign test per position, and
+    // once outside a walk stays outside.
+    const bool start_in = inside_grid(ix, iy, iz);
+    int rx = sx > 0 ? (L - 2) - ix : ix - 1;
+    int ry = sy > 0 ? (Wd - 2) - iy : iy - 1;
+    int rz = sz > 0 ? (Hz - 2) - iz : iz - 1;
+    if (!start_in) rx = -1;
     // The stepping never depends on the loaded values, only the termination does, so a
     // lead walker with the same arithmetic runs kAhead steps in front: at each position
-    // it issues the voxel's load into a register ring and records, beside it, whether
-    // the position is inside the loop bounds and which axis the step from it takes.  The
-    // trailing walk consumes value, flag and axis in order, so it repeats neither the
-    // bounds test nor the t_max comparisons.  The lead loads only voxels inside the
-    // bounds.
+    // it issues the voxel's load into a register ring and records, beside it, the
+    // position's linear index, whether it is inside the bounds and which axis the step
+    // from it takes (the Amanatides-Woo step, :384-417: the same three comparisons pick
+    // the axis).  The trailing walk consumes value, index, flag and axis in order and
+    // keeps no indices of its own.  The reference's XY..ZY (the other two indices at the
+    // last step along x, y, z) are kept as the linear index of the position each last
+    // such step left from (-1 before the first: the reference's never-assigned zeros)
+    // and decoded after the walk.  The lead loads only voxels inside the bounds.
     constexpr int kAhead = 4;
-    int ax = ix, ay = iy, az = iz, ali = li;
+    int ali = li;
     float3 atm = tm;
-    // one Amanatides-Woo step of the lead; returns the axis (0 x, 1 y, 2 z)
     auto lead_step = [&]() -> int {
-        bool bx, by, bz;
-        pick(atm, bx, by, bz);
-        ax += bx ? sx : 0;
-        ay += by ? sy : 0;
-        az += bz ? sz : 0;
-        ali += bx ? dlx : (by ? dly : dlz);
-        const float nx = atm.x + td.x, ny = atm.y + td.y, nz = atm.z + td.z;
-        atm.x = bx ? nx : atm.x;
-        atm.y = by ? ny : atm.y;
-        atm.z = bz ? nz : atm.z;
-        return bx ? 0 : (by ? 1 : 2);
+        const bool xy = atm.x < atm.y, xz = atm.x < atm.z, yz = atm.y < atm.z;
+        int axis;
+        if (xy && xz) {
+            rx -= 1;
+            ali += dlx;
+            atm.x = atm.x + td.x;
+            axis = 0;
+        } else if (!xy && yz) {
+            ry -= 1;
+            ali += dly;
+            atm.y = atm.y + td.y;
+            axis = 1;
+        } else {
+            rz -= 1;
+            ali += dlz;
+            atm.z = atm.z + td.z;
+            axis = 2;
+        }
+        return axis;
     };
     typename View::Raw ring[kAhead];
+    int ring_li[kAhead];
     int code[kAhead];  // 4: inside the bounds, | axis of the step
 #pragma unroll
     for (int k = 0; k < kAhead; ++k) {
-        const bool in = inside_grid(ax, ay, az);
+        const bool in = (rx | ry | rz) >= 0;
         ring[k] = in ? vol.raw(ali) : typename View::Raw(0);
+        ring_li[k] = ali;
         code[k] = (in ? 4 : 0) | lead_step();
     }
     float prev = 0.0f;
     float crossing = 0.f;  // the negative value met right after a positive one, or 0
+    int rec_x = -1, rec_y = -1, rec_z = -1;
     bool done = false;
-    // every step moves one index one step in a fixed direction, so the walk ends within
-    // L + Wd + Hz steps; the bound only makes that explicit
-    for (int guard = 0; !done && guard < L + Wd + Hz + 4; guard += kAhead) {
+    // Steps run in groups of kAhead without branches: a lane whose walk has ended keeps
+    // stepping with its results frozen until the group ends, and the loop is left
+    // between groups.  Every step moves one index one step in a fixed direction, so
+    // the walk ends within L + Wd + Hz steps; the bound only makes that explicit.
+    for (int guard = 0; guard < L + Wd + Hz + 4; guard += kAhead) {
 #pragma unroll
         for (int k = 0; k < kAhead; ++k) {
             const int c = code[k];
-            if (!(c & 4)) {
-                done = true;
-                break;
-            }
             const float cur = View::decode(ring[k]);
-            const bool in = inside_grid(ax, ay, az);
+            const int here = ring_li[k];
+            const bool in = (rx | ry | rz) >= 0;
             ring[k] = in ? vol.raw(ali) : typename View::Raw(0);
+            ring_li[k] = ali;
             code[k] = (in ? 4 : 0) | lead_step();
-            // the reference's four tests (:207-222) are mutually exclusive in prev
+            // the position ends the walk if it is outside the bounds, or by the
+            // reference's four tests (:207-222, mutually exclusive in prev), or as the
+            // zero crossing (a negative value right after a positive one)
+            const bool live = !done && (c & 4);
             const bool stop = prev < 0.f ? !(cur <= 0.f) : (isnan(prev) && cur < 0.f);
-            if (stop) {
-                done = true;
-                break;
-            }
-            if (prev > 0.f && cur < 0.f) {
-                // zero crossing: leave the walk with the state as it is and resolve it
-                // below, where the warp's lanes have reconverged
-                crossing = cur;
-                done = true;
-                break;
-            }
-            prev = cur;
+            const bool cross = live && !stop && prev > 0.f && cur < 0.f;
+            crossing = cross ? cur : crossing;
+            li = cross ? here : li;
+            const bool adv = live && !stop && !cross;
+            done = !adv;
+            prev = adv ? cur : prev;
             const int axis = c & 3;
-            const bool bx = axis == 0, by = axis == 1, bz = axis == 2;
-            const int ox = ix, oy = iy, oz = iz;
-            XY = bx ? oy : XY;
-            XZ = bx ? oz : XZ;
-            YX = by ? ox : YX;
-            YZ = by ? oz : YZ;
-            ZX = bz ? ox : ZX;
-            ZY = bz ? oy : ZY;
-            ix += bx ? sx : 0;
-            iy += by ? sy : 0;
-            iz += bz ? sz : 0;
-            li += bx ? dlx : (by ? dly : dlz);
+            rec_x = (adv && axis == 0) ? here : rec_x;
+            rec_y = (adv && axis == 1) ? here : rec_y;
+            rec_z = (adv && axis == 2) ? here : rec_z;
         }
+        if (done) break;
     }
     if (!(crossing < 0.f)) return;
+    // the crossing's position and the recorded indices, 1-based as in the reference
+    {
+        const int q = li / L;
+        ix = li - q * L + 1;
+        iy = q % Wd + 1;
+        iz = q / Wd + 1;
+    }
+    int XY = 0, XZ = 0, YX = 0, YZ = 0, ZX = 0, ZY = 0;
+    if (rec_x >= 0) {
+        const int q = rec_x / L;
+        XY = q % Wd + 1;
+        XZ = q / Wd + 1;
+    }
+    if (rec_y >= 0) {
+        const int q = rec_y / L;
+        YX = rec_y - q * L + 1;
+        YZ = q / Wd + 1;
+    }
+    if (rec_z >= 0) {
+        const int q = rec_z / L;
+        ZX = rec_z - q * L + 1;
+        ZY = q % Wd + 1;
+    }
     const float cur = crossing;
     const int xn = (ix - 1) - 1, xp = (ix - 1) + 1;
     const int yn = (iy - 1) - 1, yp = (iy - 1) + 1;
