@@ -789,6 +789,10 @@ __device__ __forceinline__ void solve_body(const float* __restrict__ partials, i
 // over kFixReplicas copies (block b adds to copy b % kFixReplicas), so that few atomic
 // additions queue on any one word; within a copy the 112 digits are consecutive, so a
 // block's additions and the last block's reads are whole-line (coalesced) accesses.
+// warps per block of the precision form's pass (32 / kPreciseWarps blocks per SM at
+// 64 registers a thread)
+constexpr int kPreciseWarps = 8;
+
 namespace fix {
 
 // f * 2^48 truncated toward zero as a 128-bit two's-complement integer (hi, lo); false
@@ -850,9 +854,9 @@ __device__ __forceinline__ bool digits_of(float h, float l, unsigned long long (
 __device__ __forceinline__ void gather_digits(long long* acc, long long* digits, unsigned* bad_flags,
                                               unsigned* bad_out)
 {
-    static_assert(kDigits < kExactWarps * 32, "one thread per digit and one for the flags");
+    static_assert(kDigits < kPreciseWarps * 32, "one thread per digit and one for the flags");
     const int t = threadIdx.x;
-    if (t == kExactWarps * 32 - 1) {
+    if (t == kPreciseWarps * 32 - 1) {
         // every other block's atomicOr on the flags came before its ticket
         *bad_out = __ldcg(bad_flags);
         __stcg(bad_flags, 0u);
@@ -938,14 +942,14 @@ __device__ __forceinline__ float warp_sum_transposed(const float (&v)[kIcpVals])
 }
 
 template <int MODE>
-__global__ void __launch_bounds__(kExactWarps * 32, 4) icp_precise_kernel(
+__global__ void __launch_bounds__(kPreciseWarps * 32, 32 / kPreciseWarps) icp_precise_kernel(
     const float4* __restrict__ vmap, const float4* __restrict__ nmap, const float4* __restrict__ pv,
     const float4* __restrict__ pn, Camera cam, IcpParams prm, const float* Fsrc, const float* Tsrc, State* st,
     long long* __restrict__ fixacc, int ngroups, int prefetch, int32_t* __restrict__ pair, float* sums_out)
 {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int n = cam.H * cam.W;
-    const int grp = blockIdx.x * kExactWarps + warp;
+    const int grp = blockIdx.x * kPreciseWarps + warp;
     // The vertex and normal maps are written before the frame's first ICP pass and never
     // by a pass, so after a pass (prefetch) they are loaded before waiting for it: the
     // first round of loads overlaps the previous pass's solve.
@@ -957,7 +961,7 @@ __global__ void __launch_bounds__(kExactWarps * 32, 4) icp_precise_kernel(
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     if (!prefetch) load_pair(grp * 64 + lane, n, vmap, nmap, v, nn);
     __shared__ float sF[16], sT[16];
-    __shared__ float wsum[kExactWarps][kIcpVals];
+    __shared__ float wsum[kPreciseWarps][kIcpVals];
     __shared__ unsigned long long sdig[fix::kDigits];
     __shared__ int is_last;
     if (threadIdx.x < 16) {
@@ -986,7 +990,7 @@ __global__ void __launch_bounds__(kExactWarps * 32, 4) icp_precise_kernel(
     if (threadIdx.x < kIcpVals) {
         const int k = threadIdx.x;
         float h = wsum[0][k], l = 0.f;
-        for (int w = 1; w < kExactWarps; ++w) {
+        for (int w = 1; w < kPreciseWarps; ++w) {
             float sum, e;
             two_sum(h, wsum[w][k], sum, e);
             h = sum;
@@ -1104,6 +1108,12 @@ int exact_blocks(int H, int W)
     const int g = icp_groups(H, W);
     return (g + kExactWarps - 1) / kExactWarps;
 }
+
+int precise_blocks(int H, int W)
+{
+    const int g = icp_groups(H, W);
+    return (g + kPreciseWarps - 1) / kPreciseWarps;
+}
 }  // namespace
 
 void launch_icp_iteration(const float4* vmap, const float4* nmap, const float4* pv, const float4* pn,
@@ -1120,7 +1130,7 @@ void launch_icp_iteration(const float4* vmap, const float4* nmap, const float4* 
                    prm, (float*)nullptr);
     } else if (prm.precise) {
         const int ng = icp_groups(cam.H, cam.W);
-        launch_pdl(icp_precise_kernel<0>, dim3(exact_blocks(cam.H, cam.W)), dim3(kExactWarps * 32), 0, s, vmap, nmap,
+        launch_pdl(icp_precise_kernel<0>, dim3(precise_blocks(cam.H, cam.W)), dim3(kPreciseWarps * 32), 0, s, vmap, nmap,
                    pv, pn, cam, lean_params(prm), state_F(st), state_T(st), st, fixacc, ng, after_pass ? 1 : 0,
                    (int32_t*)nullptr, (float*)nullptr);
     } else
@@ -1143,7 +1153,7 @@ void launch_icp_associate(const float4* vmap, const float4* nmap, const float4* 
                    prm, sums_out);
     } else if (prm.precise) {
         const int ng = icp_groups(cam.H, cam.W);
-        launch_pdl(icp_precise_kernel<1>, dim3(exact_blocks(cam.H, cam.W)), dim3(kExactWarps * 32), 0, s, vmap, nmap,
+        launch_pdl(icp_precise_kernel<1>, dim3(precise_blocks(cam.H, cam.W)), dim3(kPreciseWarps * 32), 0, s, vmap, nmap,
                    pv, pn, cam, lean_params(prm), F, T, st, fixacc, ng, 0, pair, sums_out);
     } else
         icp_kernel<1><<<blocks, kIcpBlock, 0, s>>>(vmap, nmap, pv, pn, cam, prm, st, F, T, partials,
