@@ -280,12 +280,12 @@ def form_config(kf, cfg, form: str):
                           solve_mode=kf.KF_SOLVE_PRECISE if f["solve"] == "precise" else kf.KF_SOLVE_REFERENCE)
 
 
-def trajectory_error(h, dev, fbytes, n_frames: int):
+def trajectory_error(h, dev, fbytes, n_frames: int, workload_name: str = "c1"):
     """Absolute trajectory error (RMS and max translation difference, mm) of this handle's
     pipeline over frames 0..n-1 against the FP64 oracle's trajectory stored in
-    tests/golden/fp64_c1_traj.npz; also the float oracle's (the reference's own
+    tests/golden/fp64_<workload>_traj.npz; also the float oracle's (the reference's own
     arithmetic) error against the same trajectory."""
-    p = ROOT / "tests" / "golden" / "fp64_c1_traj.npz"
+    p = ROOT / "tests" / "golden" / f"fp64_{workload_name}_traj.npz"
     if not p.exists():
         return None
     z = np.load(p)
@@ -296,10 +296,19 @@ def trajectory_error(h, dev, fbytes, n_frames: int):
         ptr = dev.data_ptr() + k * fbytes
         (h.initial_processing_device if k == 0 else h.incoming_frame_device)(ptr)
         poses[k] = h.pose()
-    e = np.linalg.norm(poses[:, :3, 3] - z["poses64"][:n, :3, 3], axis=1)
-    r = np.linalg.norm(z["poses32"][:n, :3, 3] - z["poses64"][:n, :3, 3], axis=1)
-    return {"frames": n, "ate_mm": float(np.sqrt(np.mean(e ** 2))), "max_mm": float(e.max()),
-            "reference_float_ate_mm": float(np.sqrt(np.mean(r ** 2)))}
+    p64 = z["poses64"][:n]
+    p32 = z["poses32"][:n].astype(np.float64)
+    e = np.linalg.norm(poses[:, :3, 3] - p64[:, :3, 3], axis=1)
+    r = np.linalg.norm(p32[:, :3, 3] - p64[:, :3, 3], axis=1)
+
+    def rpe(P):
+        # relative pose error: RMS over frames of the translation difference between the
+        # frame-to-frame motions inv(T[k-1]) T[k] of P and of the FP64 trajectory
+        d = [np.linalg.inv(P[k - 1]) @ P[k] - np.linalg.inv(p64[k - 1]) @ p64[k] for k in range(1, n)]
+        return float(np.sqrt(np.mean([np.sum(x[:3, 3] ** 2) for x in d])))
+
+    return {"frames": n, "ate_mm": float(np.sqrt(np.mean(e ** 2))), "max_mm": float(e.max()), "rpe_mm": rpe(poses),
+            "reference_float_ate_mm": float(np.sqrt(np.mean(r ** 2))), "reference_float_rpe_mm": rpe(p32)}
 
 
 def run_form(args, dist, form, cfg, frames, order, fresh, stream):
@@ -382,7 +391,7 @@ def run_form(args, dist, form, cfg, frames, order, fresh, stream):
         e2e = {"value": args.steps * dist.world / dt, "unit": "frames/s", "h2d_bytes_per_step": fbytes,
                "d2h_bytes_per_step": 64}
 
-    ate = trajectory_error(h, dev, fbytes, len(frames)) if not args.no_ate else None
+    ate = trajectory_error(h, dev, fbytes, len(frames), cfg.name) if not args.no_ate else None
     h.close()
     return {"value": args.steps * dist.world / (ms_max / 1000.0), "ms_per_step": ms_max / args.steps,
             "e2e": e2e, "stages_ms": stage_ms, "gpu_launches": launches, "clocks": clk, "ate": ate,
@@ -529,6 +538,31 @@ def run_differentiation(args) -> dict:
             "render_ms": e[0].elapsed_time(e[1]) / len(poses), "adjoint_ms": e[1].elapsed_time(e[2]) / len(poses)}
 
 
+def run_precision_c2(args, dist, stream) -> dict:
+    """Both forms on c2, the precision form's own workload: 640x480 depth into the
+    512x512x430 grid at 7 mm (113 M voxels: 902 MB as the FP32 pair, 451 MB as FP16),
+    the same seeded room, noise and frame order as c1; frames/s with the depth frames in
+    device memory, and the trajectory error of the first 48 frames against the FP64
+    oracle's (tests/golden/fp64_c2_traj.npz)."""
+    from kinect_fusion_slam_gb300 import scene
+
+    cfg = scene.config("c2")
+    sub = argparse.Namespace(**vars(args))
+    sub.steps, sub.warmup, sub.profile_frames, sub.no_e2e = 100, 3, 5, True
+    n_all = 1 + sub.warmup + sub.steps + sub.profile_frames
+    seq = scene.sequence(cfg, frames=UNIQUE_FRAMES)
+    frames = seq.depths(UNIQUE_FRAMES)
+    order = pingpong(UNIQUE_FRAMES, n_all)
+    fresh = restarts(UNIQUE_FRAMES, n_all)
+    out = {"workload": "c2: 640x480 uint16 depth, 512x512x430 TSDF @ 7 mm, single-level ICP x10",
+           "steps": sub.steps}
+    for form in ("precision", "plain"):
+        r = run_form(sub, dist, form, cfg, frames, order, fresh, stream)
+        out[form] = {"frames_per_s": r["value"], "stages_ms": r["stages_ms"], "ate": r["ate"]}
+    out["speedup_vs_fp32_form"] = out["precision"]["frames_per_s"] / out["plain"]["frames_per_s"]
+    return out
+
+
 def run_gb300(args, dist: Dist):
     import torch
 
@@ -553,6 +587,7 @@ def run_gb300(args, dist: Dist):
     if not args.no_extra_forms and dist.world == 1:
         extra["batching_c4"] = run_batching(args, stream)
         extra["differentiation_c3"] = run_differentiation(args)
+        extra["precision_c2"] = run_precision_c2(args, dist, stream)
 
     cb = None
     if dist.rank == 0 and args.gpus == 1 and not args.no_cpu_baseline:

@@ -1,9 +1,10 @@
-"""Regenerate tests/golden/fp64_c1_traj.npz -- the FP64 oracle's trajectory on the
+"""Regenerate tests/golden/fp64_<workload>_traj.npz -- the FP64 oracle's trajectory on a
 benchmark sequence.
 
-The workload is c1 (640x480 depth into the 360x360x300 grid at 10 mm) on the first 48
-frames of its seeded synthetic sequence, i.e. the first forward pass of the benchmark's
-frame order.  Two trajectories are stored, both from the CPU oracles in oracle/:
+Workload c1 (default): 640x480 depth into the 360x360x300 grid at 10 mm; workload c2:
+the precision form's 512x512x430 grid at 7 mm.  Either way the first 48 frames of its
+seeded synthetic sequence, i.e. the first forward pass of the benchmark's frame order.
+Two trajectories are stored, both from the CPU oracles in oracle/:
 
   poses64  the FP64 oracle (kf_oracle64.cpp): the reference's algorithm in double
   poses32  the float oracle (kf_oracle.cpp): the reference's own float arithmetic,
@@ -13,7 +14,7 @@ The benchmark compares the GPU trajectories of both forms with poses64 (the abso
 trajectory error of the precision form), and poses32 against poses64 gives the
 reference's own sensitivity to arithmetic precision on this sequence.
 
-    python tests/golden/make_fp64_traj.py
+    python tests/golden/make_fp64_traj.py [c1|c2]
 """
 from __future__ import annotations
 
@@ -29,11 +30,11 @@ sys.path.insert(0, str(ROOT))
 FRAMES = 48
 
 
-def main() -> None:
+def main(workload: str = "c1") -> None:
     from kinect_fusion_slam_gb300 import scene
     from oracle.pyoracle import GridSpec, Oracle
 
-    cfg = scene.config("c1")
+    cfg = scene.config(workload)
     seq = scene.sequence(cfg, frames=FRAMES)
     depths = seq.depths(FRAMES)
     g = cfg.grid
@@ -52,11 +53,11 @@ def main() -> None:
         poses32[k] = p32.pose
     p64.close()
     p32.close()
-    np.savez_compressed(HERE / "fp64_c1_traj.npz", poses64=poses64, poses32=poses32, frames=FRAMES,
-                        workload="c1 frames 0..47")
+    np.savez_compressed(HERE / f"fp64_{workload}_traj.npz", poses64=poses64, poses32=poses32, frames=FRAMES,
+                        workload=f"{workload} frames 0..47")
     err = np.linalg.norm(poses32[:, :3, 3] - poses64[:, :3, 3], axis=1)
     print(f"written; float oracle vs FP64 oracle: ATE {np.sqrt(np.mean(err ** 2)):.3f} mm, max {err.max():.3f} mm")
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1] if len(sys.argv) > 1 else "c1")

@@ -7,6 +7,8 @@ FP64 oracle (oracle/kf_oracle64.cpp: the same algorithm in double), stage by sta
 
 * the TSDF and weights after integrating frames at fixed poses (open loop),
 * the predicted surface after a ray cast at a fixed pose,
+* both of these on the precision form's own workload c2 (512x512x430 at 7 mm), with the
+  TSDF's RMS error and the rendered depth's RMS error,
 * the 27 normal-equation sums of one ICP association, against the exact sum of the
   per-pixel terms of its correspondences (which match the plain form's up to pixels at
   a rounding boundary),
@@ -96,6 +98,66 @@ def test_fp16_prediction_against_fp64_oracle(oracle, small_seq):
     # well under a millimetre
     assert np.median(d) <= 0.5, np.median(d)
     assert np.percentile(d, 95) <= 3.0, np.percentile(d, 95)
+
+
+@pytest.fixture(scope="module")
+def c2_seq():
+    """The precision form's own workload c2: 640x480 depth into 512x512x430 at 7 mm."""
+    from kinect_fusion_slam_gb300 import scene
+
+    seq = scene.sequence(scene.config("c2"), frames=3)
+    return seq, seq.depths(3)
+
+
+def _camera_depth(pred, T):
+    """Camera-frame depth (mm) of world-space predicted points under pose T; NaN off hits."""
+    P = pred[:3].reshape(3, -1).astype(np.float64)
+    Ti = np.linalg.inv(T.astype(np.float64))
+    z = Ti[2, :3] @ P + Ti[2, 3]
+    z[pred[2].ravel() == 0] = np.nan
+    return z
+
+
+def test_c2_tsdf_and_rendered_depth_against_fp64_oracle(oracle, c2_seq):
+    """c2 at full size (113 M voxels): three frames integrated at the sequence's poses by
+    the precision form, the FP64 oracle and the float oracle (the plain form's
+    arithmetic).  The FP16 TSDF's error against FP64 (RMS and 0.999 quantile; the
+    maximum is reported) stays within the float pipeline's own plus FP16 rounding; a ray
+    cast at the last pose renders depth whose RMS error against the FP64 oracle's (over
+    pixels both hit on the same surface, |difference| < 2 voxels) is sub-millimetre and
+    within 0.25 mm of the float pipeline's."""
+    seq, depths = c2_seq
+    gs = grid_spec(seq.cfg.grid)
+    h, p64, (t32, w32) = _integrate_open_loop(oracle, seq, depths, [0, 1, 2])
+    t16, w16 = h.volume()
+    t64, w64 = p64.volume()
+    both = ~np.isnan(w16) & ~np.isnan(w64)
+    assert both.sum() > 1_000_000
+    same_w = both & (w16 == w64) & (w32 == w64)
+    assert same_w.sum() >= 0.99 * both.sum()
+    e16 = np.abs(t16[same_w].astype(np.float64) - t64[same_w])
+    e32 = np.abs(t32[same_w].astype(np.float64) - t64[same_w])
+    rms16, rms32 = np.sqrt(np.mean(e16 ** 2)), np.sqrt(np.mean(e32 ** 2))
+    q16, q32 = np.quantile(e16, 0.999), np.quantile(e32, 0.999)
+    stats = dict(rms16=rms16, rms32=rms32, q16=q16, q32=q32, max16=e16.max(), max32=e32.max())
+    assert q16 <= q32 + 1.5e-3, stats
+    assert rms16 <= rms32 + 5e-4, stats
+
+    T = seq.poses[2].astype(np.float32)
+    h.ray_casting()
+    pred16 = h.predicted()
+    p64.raycast_frame()
+    pred64 = p64.prediction()
+    Ki = oracle.inv3(seq.K)
+    pred32, _ = oracle.raycast(gs, oracle.depth_ingest(depths[2]), Ki, T, t32)
+    z16, z32, z64 = (_camera_depth(p, T) for p in (pred16, pred32, pred64))
+    vd = seq.cfg.grid.voxel_size
+    same16 = np.abs(z16 - z64) < 2 * vd
+    same32 = np.abs(z32 - z64) < 2 * vd
+    assert same16.sum() > 100_000 and same16.sum() >= 0.97 * same32.sum(), (same16.sum(), same32.sum())
+    r16 = np.sqrt(np.mean((z16 - z64)[same16] ** 2))
+    r32 = np.sqrt(np.mean((z32 - z64)[same32] ** 2))
+    assert r16 <= 1.0 and r16 <= r32 + 0.25, (r16, r32, stats)
 
 
 def _tri(r, s):
