@@ -11,7 +11,14 @@ backwards; the pipeline starts over (reset + InitialProcessing) at the start of 
   value   frames/s with the depth frames already in device memory (all ranks)
   e2e     frames/s through the C ABI with host buffers: each frame's uint16 depth is
           copied from pinned host memory and the pose read back to the host
-  roofline, cpu_baseline, clocks, stage times: see the design doc
+  roofline   the dominant stage's algorithmic bytes per frame over its live time,
+             against the measured copy bandwidth; DRAM traffic from the committed ncu
+             launch lists (profiles/ncu_traffic.txt)
+  cpu_baseline  the reference's kernel bodies on the host cores, a bounded sample
+  clocks     SM clock and throttle reasons sampled during the timed region
+  stages_ms  per-stage device time of a few frames (CUDA events inside the graph)
+  ate        trajectory error against the FP64 oracle's trajectory (golden file)
+  fp32_form, precision_c2, batching_c4, differentiation_c3: the other forms/workloads
 
 --impl reference times the reference's own kernel bodies compiled for the host CPU
 (oracle/_ref, or the oracle restatement where that could not be built) on the same
