@@ -18,7 +18,8 @@ backwards; the pipeline starts over (reset + InitialProcessing) at the start of 
   clocks     SM clock and throttle reasons sampled during the timed region
   stages_ms  per-stage device time of a few frames (CUDA events inside the graph)
   ate        trajectory error against the FP64 oracle's trajectory (golden file)
-  fp32_form, precision_c2, batching_c4, differentiation_c3: the other forms/workloads
+  fp32_form, precision_c2, pyramid_c1, batching_c4, differentiation_c3: the other
+             forms and workloads
 
 --impl reference times the reference's own kernel bodies compiled for the host CPU
 (oracle/_ref, or the oracle restatement where that could not be built) on the same
@@ -277,14 +278,14 @@ FORMS = {
 }
 
 
-def form_config(kf, cfg, form: str):
+def form_config(kf, cfg, form: str, **extra):
     g, cam = cfg.grid, cfg.camera
     f = FORMS[form]
     return kf.make_config(height=cam.height, width=cam.width, dims=g.dims, grid_start=g.start,
                           voxel_size=g.voxel_size,
                           tsdf_storage=kf.KF_TSDF_F16 if f["tsdf"] == "f16" else kf.KF_TSDF_F32,
                           icp_reduction=kf.KF_REDUCE_TREE if f["reduction"] == "tree" else kf.KF_REDUCE_REFERENCE_ORDER,
-                          solve_mode=kf.KF_SOLVE_PRECISE if f["solve"] == "precise" else kf.KF_SOLVE_REFERENCE)
+                          solve_mode=kf.KF_SOLVE_PRECISE if f["solve"] == "precise" else kf.KF_SOLVE_REFERENCE, **extra)
 
 
 def trajectory_error(h, dev, fbytes, n_frames: int, workload_name: str = "c1"):
@@ -318,13 +319,13 @@ def trajectory_error(h, dev, fbytes, n_frames: int, workload_name: str = "c1"):
             "reference_float_ate_mm": float(np.sqrt(np.mean(r ** 2))), "reference_float_rpe_mm": rpe(p32)}
 
 
-def run_form(args, dist, form, cfg, frames, order, fresh, stream):
+def run_form(args, dist, form, cfg, frames, order, fresh, stream, **extra):
     import torch
 
     import kinect_fusion_slam_gb300 as kf
 
     cam = cfg.camera
-    h = kf.Handle(form_config(kf, cfg, form))
+    h = kf.Handle(form_config(kf, cfg, form, **extra))
     K = cfg.camera.K_reference()
     h.set_intrinsics(K[0, 0], K[1, 1], K[0, 2], K[1, 2])
     h.set_stream(stream.cuda_stream)
@@ -570,6 +571,28 @@ def run_precision_c2(args, dist, stream) -> dict:
     return out
 
 
+def run_pyramid_c1(args, dist, stream) -> dict:
+    """Both forms on c1 with the three-level ICP pyramid of the workload's description
+    (10/5/4 iterations, coarsest level first).  The reference has one level (10
+    iterations), which the headline line and its reference arm keep; this times the
+    pyramid form beside it, with the depth frames in device memory."""
+    from kinect_fusion_slam_gb300 import scene
+
+    cfg = scene.config("c1")
+    sub = argparse.Namespace(**vars(args))
+    sub.steps, sub.warmup, sub.profile_frames, sub.no_e2e, sub.no_ate = 100, 3, 5, True, True
+    n_all = 1 + sub.warmup + sub.steps + sub.profile_frames
+    seq = scene.sequence(cfg, frames=UNIQUE_FRAMES)
+    frames = seq.depths(UNIQUE_FRAMES)
+    order = pingpong(UNIQUE_FRAMES, n_all)
+    fresh = restarts(UNIQUE_FRAMES, n_all)
+    out = {"workload": "c1 with a 3-level ICP pyramid (10/5/4 iterations)", "steps": sub.steps}
+    for form in ("precision", "plain"):
+        r = run_form(sub, dist, form, cfg, frames, order, fresh, stream, icp_levels=3, icp_iterations=(10, 5, 4))
+        out[form] = {"frames_per_s": r["value"], "stages_ms": r["stages_ms"]}
+    return out
+
+
 def run_gb300(args, dist: Dist):
     import torch
 
@@ -595,6 +618,7 @@ def run_gb300(args, dist: Dist):
         extra["batching_c4"] = run_batching(args, stream)
         extra["differentiation_c3"] = run_differentiation(args)
         extra["precision_c2"] = run_precision_c2(args, dist, stream)
+        extra["pyramid_c1"] = run_pyramid_c1(args, dist, stream)
 
     cb = None
     if dist.rank == 0 and args.gpus == 1 and not args.no_cpu_baseline:

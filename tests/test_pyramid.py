@@ -60,3 +60,35 @@ def test_pyramid_pipeline_bit_exact_with_oracle(oracle, small_seq):
     to, wo = p.volume()
     assert np.array_equal(np.isnan(w), np.isnan(wo))
     assert np.array_equal(t[~np.isnan(t)].view(np.uint32), to[~np.isnan(to)].view(np.uint32))
+
+
+@pytest.mark.gpu
+def test_precision_form_pyramid_tracks_like_the_plain_pyramid(oracle, small_seq):
+    """The precision form's one-pass ICP (fused association, exact fixed-point sums,
+    FP64 solve) on the same 3-level pyramid: every level's passes find correspondences,
+    and over three tracked frames its distance from the sequence's true poses stays
+    within the float pyramid's own plus a millimetre (the tracker turns last-bit
+    differences into millimetres within a few frames, so the two forms are compared
+    through the ground truth rather than with each other)."""
+    seq, depths = small_seq
+    H, W = depths.shape[1:]
+    g = seq.cfg.grid
+    h = kf.Handle(kf.make_config(height=H, width=W, dims=g.dims, grid_start=g.start, voxel_size=g.voxel_size,
+                                 icp_levels=3, icp_iterations=(10, 5, 4), tsdf_storage=kf.KF_TSDF_F16,
+                                 solve_mode=kf.KF_SOLVE_PRECISE, icp_reduction=kf.KF_REDUCE_TREE))
+    K = seq.K
+    h.set_intrinsics(K[0, 0], K[1, 1], K[0, 2], K[1, 2])
+    p = oracle.pipeline(H, W, grid_spec(g), K)
+    p.set_pyramid(3, [10, 5, 4], band=90.0)
+    h.initial_processing(depths[0])
+    p.initial(depths[0])
+    for k in range(1, 4):
+        h.incoming_frame(depths[k])
+        p.incoming(depths[k])
+        gt = seq.poses[k].astype(np.float64)
+        eg = np.linalg.norm(h.pose().astype(np.float64)[:3, 3] - gt[:3, 3])
+        eo = np.linalg.norm(p.pose.astype(np.float64)[:3, 3] - gt[:3, 3])
+        assert eg <= eo + 1.0 + 0.5 * eo, (k, eg, eo)
+    assert h.kernels_per_frame() == 1 + 3 * 2 + 19 + 3
+    nc, _ = h.icp_stats()
+    assert len(nc) == 19 and min(nc) > 10
