@@ -1,7 +1,8 @@
 """Build recipe of the kinfu_gb300 shared library (sm_103a only).
 
 Compiles the CUDA translation units under ``csrc/`` in parallel with nvcc and links
-them into ``kinect_fusion_slam_gb300/lib/libkinfu_gb300.so`` (in-tree, git-ignored).
+them into ``kinect_fusion_slam_gb300/lib/libkinfu_gb300.so`` (in-tree, git-ignored),
+then the headless C++ frame loop ``driver/kinfu_run.cpp`` into ``lib/kinfu_run``.
 
 Device code is compiled with ``-fmad=false`` and host code with
 ``-ffp-contract=off``: the plain FP32 form reproduces the reference's per-element
@@ -24,6 +25,8 @@ INCLUDE = PKG.parent / "include"
 OUT_DIR = PKG / "lib"
 BUILD_DIR = PKG / "_build"
 LIB = OUT_DIR / "libkinfu_gb300.so"
+DRIVER_SRC = PKG / "driver" / "kinfu_run.cpp"
+DRIVER = OUT_DIR / "kinfu_run"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = [
@@ -54,7 +57,34 @@ def _stale(target: Path, deps) -> bool:
     return any(Path(d).stat().st_mtime > t for d in deps)
 
 
+def build_driver(force: bool = False, verbose: bool = False) -> Path:
+    """The headless C++ frame loop (driver/kinfu_run.cpp over include/kinfu_pipeline.hpp),
+    linked against the library with an $ORIGIN run path."""
+    deps = [DRIVER_SRC, LIB, INCLUDE / "kinfu_pipeline.hpp", INCLUDE / "kinfu_gb300.h"]
+    if not force and not _stale(DRIVER, deps):
+        return DRIVER
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if not cxx:
+        raise RuntimeError("no C++ compiler for the kinfu_run driver")
+    tmp = DRIVER.with_suffix(".tmp")
+    cmd = [cxx, "-std=c++17", "-O2", "-Wall", "-I", str(INCLUDE), str(DRIVER_SRC), "-L", str(OUT_DIR),
+           "-lkinfu_gb300", "-Wl,-rpath,$ORIGIN", "-o", str(tmp)]
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"kinfu_run failed to build:\n{r.stdout}\n{r.stderr}")
+    os.replace(tmp, DRIVER)
+    return DRIVER
+
+
 def build(force: bool = False, verbose: bool = False, extra: list[str] | None = None) -> Path:
+    lib = build_library(force, verbose, extra)
+    build_driver(force, verbose)
+    return lib
+
+
+def build_library(force: bool = False, verbose: bool = False, extra: list[str] | None = None) -> Path:
     srcs = sources()
     deps = srcs + headers() + [Path(__file__)]
     if not force and not _stale(LIB, deps):
