@@ -408,6 +408,34 @@ def test_pipeline_free_running_c0(oracle, c0_seq):
     assert np.array_equal(h.ray_casting(), hit_o)
 
 
+def test_pipeline_free_running_c2(oracle):
+    """The largest grid of the workloads, c2 (512x512x430 @ 7 mm: 113 M voxels, linear
+    indices past 2^26), plain form: four frames free-running on the GPU and in the float
+    oracle give the same poses, voxels, weights and hit indices bit for bit."""
+    from kinect_fusion_slam_gb300 import scene
+
+    seq = scene.sequence("c2", frames=4)
+    depths = seq.depths(4)
+    gs = grid_spec(seq.cfg.grid)
+    assert gs.nvox > 1 << 26
+    h = make_handle(seq)
+    o = oracle.pipeline(480, 640, gs, seq.K)
+    h.initial_processing(depths[0])
+    o.initial(depths[0])
+    for k in range(1, len(depths)):
+        h.incoming_frame(depths[k])
+        o.incoming(depths[k])
+        assert np.array_equal(h.pose().view(np.uint32), o.pose.view(np.uint32)), f"frame {k}"
+    tg, wg = h.volume()
+    to, wo = o.volume()
+    assert_volume_parity(tg, wg, to, wo)
+    assert int((~np.isnan(wo)).sum()) > 1_000_000
+    _, hit_o = o.prediction()
+    hit_g = h.ray_casting()
+    assert np.array_equal(hit_g, hit_o) and int((hit_o >= 0).sum()) > 100_000
+    h.close()
+
+
 def test_graph_and_eager_agree(small_seq):
     seq, depths = small_seq
     poses = []
