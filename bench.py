@@ -395,6 +395,7 @@ def run_form(args, dist, form, cfg, frames, order, fresh, stream, **extra):
             else:
                 h.incoming_frame_ptr(ptr)
             h.pose()
+        h.synchronize()  # the last frame's integration and ray cast (the pose is read at its ICP's end)
         dt = dist.max(time.perf_counter() - t0)
         e2e = {"value": args.steps * dist.world / dt, "unit": "frames/s", "h2d_bytes_per_step": fbytes,
                "d2h_bytes_per_step": 64}

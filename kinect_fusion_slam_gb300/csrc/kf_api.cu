@@ -48,8 +48,9 @@ T* field_ptr(State* st, size_t offset)
 void destroy_graphs(kf_handle* h)
 {
     if (h->g_incoming) cudaGraphExecDestroy(h->g_incoming);
+    if (h->g_incoming_alt) cudaGraphExecDestroy(h->g_incoming_alt);
     if (h->g_initial) cudaGraphExecDestroy(h->g_initial);
-    h->g_incoming = h->g_initial = nullptr;
+    h->g_incoming = h->g_incoming_alt = h->g_initial = nullptr;
 }
 
 bool validate(const kf_config* c, std::string& why)
@@ -142,6 +143,36 @@ kf_status upload_raw(kf_handle* h, const uint16_t* depth)
     return KF_OK;
 }
 
+bool is_pinned(const void* p)
+{
+    cudaPointerAttributes attr{};
+    const bool pinned = cudaPointerGetAttributes(&attr, p) == cudaSuccess &&
+                        (attr.type == cudaMemoryTypeHost || attr.type == cudaMemoryTypeManaged);
+    cudaGetLastError();
+    return pinned;
+}
+
+// the stream work enqueued so far is the latest to read buffer b
+void raw_used(kf_handle* h, int b) { cudaEventRecord(h->ev_raw_free[b], h->stream); }
+
+// A pinned host frame's copy into the other raw buffer on copy_stream, after the latest
+// work that read that buffer (the frame before the previous one, normally long done) and
+// concurrent with the previous frame's work; the frame's stream waits for the copy.
+// (The host wrote the frame before the call, so the copy needs no stream order.)
+// Returns the buffer.
+kf_status upload_raw_async(kf_handle* h, const uint16_t* depth, cudaMemcpyKind kind, int& buf)
+{
+    const size_t bytes = sizeof(uint16_t) * h->cam.H * h->cam.W;
+    buf = h->raw_turn ^ 1;
+    uint16_t* dst = buf ? h->d_raw_alt : h->d_raw;
+    KF_CUDA(h, cudaStreamWaitEvent(h->copy_stream, h->ev_raw_free[buf], 0));
+    KF_CUDA(h, cudaMemcpyAsync(dst, depth, bytes, kind, h->copy_stream));
+    KF_CUDA(h, cudaEventRecord(h->ev_copied, h->copy_stream));
+    KF_CUDA(h, cudaStreamWaitEvent(h->stream, h->ev_copied, 0));
+    h->raw_turn = buf;
+    return KF_OK;
+}
+
 // ---- stage enqueuers (no synchronisation) ----
 void enq_ingest(kf_handle* h, const uint16_t* raw, bool init_icp, bool normals)
 {
@@ -219,6 +250,24 @@ void stamp(kf_handle* h, int k)
 // bilateral call site the reference leaves commented out sits after the vertex map
 // (kinfu_pipeline.cpp:141-145): when enabled here it filters the depth that ICP,
 // integration and ray casting use, in the same place.
+// ev_pose where the frame's pose is final: recorded on a side branch forked from the
+// frame's stream at this point (an external event node when captured) and joined back
+// by join_pose at the end of the frame
+void mark_pose(kf_handle* h)
+{
+    cudaEventRecord(h->ev_fork, h->stream);
+    cudaStreamWaitEvent(h->pose_stream, h->ev_fork, 0);
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaStreamIsCapturing(h->stream, &cs);
+    if (cs == cudaStreamCaptureStatusActive)
+        cudaEventRecordWithFlags(h->ev_pose, h->pose_stream, cudaEventRecordExternal);
+    else
+        cudaEventRecord(h->ev_pose, h->pose_stream);
+    cudaEventRecord(h->ev_join, h->pose_stream);
+}
+
+void join_pose(kf_handle* h) { cudaStreamWaitEvent(h->stream, h->ev_join, 0); }
+
 void enq_incoming(kf_handle* h, const uint16_t* raw)
 {
     stamp(h, 0);
@@ -226,28 +275,32 @@ void enq_incoming(kf_handle* h, const uint16_t* raw)
     if (h->cfg.bilateral) enq_bilateral(h);
     stamp(h, 1);
     enq_icp(h);
+    mark_pose(h);
     stamp(h, 2);
     enq_integrate(h, false);
     stamp(h, 3);
     enq_raycast(h, h->d_hit);
     stamp(h, 4);
+    join_pose(h);
 }
 
 // InitialProcessing after the depth upload (kinfu_pipeline.cpp:93-115)
 void enq_initial(kf_handle* h, const uint16_t* raw)
 {
+    mark_pose(h);  // InitialProcessing keeps the pose
     enq_ingest(h, raw, false, true);
     enq_integrate(h, true);
     enq_raycast(h, h->d_hit);
+    join_pose(h);
 }
 
-kf_status run_captured(kf_handle* h, cudaGraphExec_t& exec, bool incoming)
+kf_status run_captured(kf_handle* h, cudaGraphExec_t& exec, bool incoming, const uint16_t* raw)
 {
     if (!h->cfg.use_graphs) {
         if (incoming)
-            enq_incoming(h, h->d_raw);
+            enq_incoming(h, raw);
         else
-            enq_initial(h, h->d_raw);
+            enq_initial(h, raw);
         KF_CHECK_LAUNCH(h);
         return KF_OK;
     }
@@ -255,9 +308,9 @@ kf_status run_captured(kf_handle* h, cudaGraphExec_t& exec, bool incoming)
         cudaGraph_t graph = nullptr;
         KF_CUDA(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
         if (incoming)
-            enq_incoming(h, h->d_raw);
+            enq_incoming(h, raw);
         else
-            enq_initial(h, h->d_raw);
+            enq_initial(h, raw);
         cudaError_t le = cudaGetLastError();
         cudaError_t ce = cudaStreamEndCapture(h->stream, &graph);
         if (le != cudaSuccess || ce != cudaSuccess) {
@@ -319,6 +372,7 @@ kf_status dalloc(kf_handle* h, T** p, size_t count)
 #define KF_HANDLE(h)                                    \
     do {                                                \
         if (!(h)) return KF_ERR_INVALID_ARGUMENT;       \
+        ++(h)->calls;                                   \
         cudaSetDevice((h)->device);                     \
     } while (0)
 
@@ -326,6 +380,7 @@ kf_status allocate(kf_handle* h)
 {
     const size_t HW = (size_t)h->cam.H * h->cam.W;
     KF_TRY(dalloc(h, &h->d_raw, HW));
+    KF_TRY(dalloc(h, &h->d_raw_alt, HW));
     KF_TRY(dalloc(h, &h->d_depth, HW));
     KF_TRY(dalloc(h, &h->d_depth_tmp, HW));
     KF_TRY(dalloc(h, &h->d_vmap, HW));
@@ -366,6 +421,14 @@ kf_status allocate(kf_handle* h)
     KF_CUDA(h, cudaMallocHost((void**)&h->h_raw, sizeof(uint16_t) * HW));
     KF_CUDA(h, cudaMallocHost((void**)&h->h_state, sizeof(State)));
     for (auto& e : h->ev) KF_CUDA(h, cudaEventCreate(&e));
+    KF_CUDA(h, cudaEventCreateWithFlags(&h->ev_pose, cudaEventDisableTiming));
+    KF_CUDA(h, cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming));
+    KF_CUDA(h, cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming));
+    KF_CUDA(h, cudaStreamCreateWithFlags(&h->aux_stream, cudaStreamNonBlocking));
+    KF_CUDA(h, cudaStreamCreateWithFlags(&h->pose_stream, cudaStreamNonBlocking));
+    KF_CUDA(h, cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
+    KF_CUDA(h, cudaEventCreateWithFlags(&h->ev_copied, cudaEventDisableTiming));
+    for (auto& e : h->ev_raw_free) KF_CUDA(h, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     return KF_OK;
 }
 
@@ -408,7 +471,7 @@ kf_status reset_state(kf_handle* h)
 void free_all(kf_handle* h)
 {
     destroy_graphs(h);
-    void* dev[] = {h->d_raw, h->d_depth, h->d_depth_tmp, h->d_vmap, h->d_nmap, h->d_pv, h->d_pn, h->d_hit,
+    void* dev[] = {h->d_raw, h->d_raw_alt, h->d_depth, h->d_depth_tmp, h->d_vmap, h->d_nmap, h->d_pv, h->d_pn, h->d_hit,
                    h->d_pair, h->d_tab, h->d_tsdf, h->d_weight, h->d_vol16, h->d_state, h->d_partials, h->d_groups,
                    h->d_fixacc,
                    h->d_tiles, h->d_mats,
@@ -424,6 +487,10 @@ void free_all(kf_handle* h)
     if (h->h_state) cudaFreeHost(h->h_state);
     for (auto& e : h->ev)
         if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : {h->ev_pose, h->ev_fork, h->ev_join, h->ev_copied, h->ev_raw_free[0], h->ev_raw_free[1]})
+        if (e) cudaEventDestroy(e);
+    for (cudaStream_t st : {h->aux_stream, h->pose_stream, h->copy_stream})
+        if (st) cudaStreamDestroy(st);
     if (h->own_stream) cudaStreamDestroy(h->own_stream);
 }
 
@@ -592,8 +659,16 @@ kf_status kf_get_pose(kf_handle* h, float T[16])
     if (!T) return fail(h, KF_ERR_INVALID_ARGUMENT, "null pose");
     // T and the error flag are adjacent in State: one small copy reads both
     constexpr size_t bytes = offsetof(State, error) + sizeof(int);
-    KF_CUDA(h, cudaMemcpyAsync(h->h_state, h->d_state, bytes, cudaMemcpyDeviceToHost, h->stream));
-    KF_CUDA(h, cudaStreamSynchronize(h->stream));
+    if (h->pose_call + 1 == h->calls) {
+        // right after a frame call: the pose is final at ev_pose; integration and the
+        // ray cast go on in the stream (no kernel after the ICP writes T or the flag)
+        KF_CUDA(h, cudaStreamWaitEvent(h->aux_stream, h->ev_pose, 0));
+        KF_CUDA(h, cudaMemcpyAsync(h->h_state, h->d_state, bytes, cudaMemcpyDeviceToHost, h->aux_stream));
+        KF_CUDA(h, cudaStreamSynchronize(h->aux_stream));
+    } else {
+        KF_CUDA(h, cudaMemcpyAsync(h->h_state, h->d_state, bytes, cudaMemcpyDeviceToHost, h->stream));
+        KF_CUDA(h, cudaStreamSynchronize(h->stream));
+    }
     std::memcpy(T, h->h_state->T, sizeof(float) * 16);
     if (h->h_state->error) {
         const int zero = 0;
@@ -637,7 +712,9 @@ kf_status kf_initial_processing(kf_handle* h, const uint16_t* depth)
     KF_HANDLE(h);
     if (!depth) return fail(h, KF_ERR_INVALID_ARGUMENT, "null depth");
     KF_TRY(upload_raw(h, depth));
-    KF_TRY(run_captured(h, h->g_initial, false));
+    KF_TRY(run_captured(h, h->g_initial, false, h->d_raw));
+    raw_used(h, 0);
+    h->pose_call = h->calls;
     return KF_OK;
 }
 
@@ -645,9 +722,18 @@ kf_status kf_incoming_frame(kf_handle* h, const uint16_t* depth)
 {
     KF_HANDLE(h);
     if (!depth) return fail(h, KF_ERR_INVALID_ARGUMENT, "null depth");
-    KF_TRY(upload_raw(h, depth));
-    KF_TRY(run_captured(h, h->g_incoming, true));
+    if (is_pinned(depth)) {
+        int buf = 0;
+        KF_TRY(upload_raw_async(h, depth, cudaMemcpyHostToDevice, buf));
+        KF_TRY(run_captured(h, buf ? h->g_incoming_alt : h->g_incoming, true, buf ? h->d_raw_alt : h->d_raw));
+        raw_used(h, buf);
+    } else {
+        KF_TRY(upload_raw(h, depth));
+        KF_TRY(run_captured(h, h->g_incoming, true, h->d_raw));
+        raw_used(h, 0);
+    }
     h->frame_timed = h->timing;
+    h->pose_call = h->calls;
     return KF_OK;
 }
 
@@ -657,7 +743,9 @@ kf_status kf_initial_processing_device(kf_handle* h, const uint16_t* depth_dev)
     if (!depth_dev) return fail(h, KF_ERR_INVALID_ARGUMENT, "null depth");
     KF_CUDA(h, cudaMemcpyAsync(h->d_raw, depth_dev, sizeof(uint16_t) * h->cam.H * h->cam.W, cudaMemcpyDeviceToDevice,
                                h->stream));
-    KF_TRY(run_captured(h, h->g_initial, false));
+    KF_TRY(run_captured(h, h->g_initial, false, h->d_raw));
+    raw_used(h, 0);
+    h->pose_call = h->calls;
     return KF_OK;
 }
 
@@ -665,10 +753,13 @@ kf_status kf_incoming_frame_device(kf_handle* h, const uint16_t* depth_dev)
 {
     KF_HANDLE(h);
     if (!depth_dev) return fail(h, KF_ERR_INVALID_ARGUMENT, "null depth");
+    // in stream order: the caller may have produced the frame on this stream
     KF_CUDA(h, cudaMemcpyAsync(h->d_raw, depth_dev, sizeof(uint16_t) * h->cam.H * h->cam.W, cudaMemcpyDeviceToDevice,
                                h->stream));
-    KF_TRY(run_captured(h, h->g_incoming, true));
+    KF_TRY(run_captured(h, h->g_incoming, true, h->d_raw));
+    raw_used(h, 0);
     h->frame_timed = h->timing;
+    h->pose_call = h->calls;
     return KF_OK;
 }
 
@@ -1017,6 +1108,7 @@ kf_status kf_set_depth_u16(kf_handle* h, const uint16_t* depth)
     if (!depth) return fail(h, KF_ERR_INVALID_ARGUMENT, "null depth");
     KF_TRY(upload_raw(h, depth));
     enq_ingest(h, h->d_raw, false, false);
+    raw_used(h, 0);
     KF_CHECK_LAUNCH(h);
     KF_CUDA(h, cudaStreamSynchronize(h->stream));
     return KF_OK;

@@ -60,4 +60,29 @@ struct kf_handle {
     float stage_ms[5] = {};
     bool frame_timed = false;
     std::string err;
+
+    // Early pose read-back: a frame call records ev_pose where the frame's pose is final
+    // (after the ICP; at once for InitialProcessing), and kf_get_pose right after it
+    // copies the pose on aux_stream once that event has passed, while integration and
+    // the ray cast still run.  calls counts the API calls on the handle; pose_call is
+    // the count after the latest frame call, so any call in between falls back to the
+    // full stream synchronisation.
+    cudaEvent_t ev_pose = nullptr;
+    cudaStream_t aux_stream = nullptr;
+    // the side branch that records ev_pose, so that the frame's kernel chain (and its
+    // programmatic launches) is not cut by an event node
+    cudaStream_t pose_stream = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+
+    // Pinned host frames are copied on copy_stream into one of two raw buffers (d_raw,
+    // d_raw_alt; g_incoming and g_incoming_alt read them), so a frame's copy overlaps the
+    // previous frame's integration and ray cast.  ev_raw_free[b] marks the end of the
+    // latest stream work that reads buffer b; ev_copied the end of a copy.
+    uint16_t* d_raw_alt = nullptr;
+    cudaGraphExec_t g_incoming_alt = nullptr;
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t ev_copied = nullptr, ev_raw_free[2] = {};
+    int raw_turn = 0;  // buffer of the latest pinned frame
+    mutable unsigned long long calls = 0;
+    unsigned long long pose_call = 0;
 };
