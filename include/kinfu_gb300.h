@@ -100,6 +100,9 @@ kf_status kf_set_intrinsics(kf_handle* h, float fx, float fy, float cx, float cy
 kf_status kf_get_intrinsics(const kf_handle* h, float K[9]);
 /* extrinsic_matrix (kinfu_pipeline.h:18): 4x4 row-major camera-to-world, mm */
 kf_status kf_set_pose(kf_handle* h, const float T[16]);
+/* Right after a frame call, waits only until that frame's pose is final (the end of its
+ * ICP; integration and the ray cast go on in the stream); otherwise waits for all work
+ * on the handle's stream. */
 kf_status kf_get_pose(kf_handle* h, float T[16]);
 /* resets the volume to NaN and the pose to identity; asynchronous on the handle's
  * stream, like the frame calls (the next frame call is kf_initial_processing) */
@@ -107,15 +110,19 @@ kf_status kf_reset(kf_handle* h);
 
 /* ---- frame loop (KinfuPipeline) --------------------------------------------------
  * depth: H*W uint16 millimetres (the contents of dep%04d.dat); host pointer, pinned
- * or pageable.  Range filtering to [min_depth, max_depth] happens on the device. */
+ * or pageable.  Range filtering to [min_depth, max_depth] happens on the device.  A
+ * pinned frame of kf_incoming_frame is copied on a second stream, overlapping the
+ * previous frame's work; the caller may reuse the buffer once kf_get_pose or
+ * kf_synchronize has returned. */
 /* InitialProcessing (kinfu_pipeline.cpp:91-119): integrate at the current pose (first
  * frame semantics) and ray cast the surface prediction */
 kf_status kf_initial_processing(kf_handle* h, const uint16_t* depth);
 /* IncomingFrameProcessing (kinfu_pipeline.cpp:121-193): vertex/normal map, ICP,
- * integration, ray cast.  Asynchronous on the handle's stream; kf_get_pose or
- * kf_synchronize waits for it. */
+ * integration, ray cast.  Asynchronous on the handle's stream; kf_synchronize (and
+ * every call reading images or the volume) waits for it, kf_get_pose for its pose. */
 kf_status kf_incoming_frame(kf_handle* h, const uint16_t* depth);
-/* same as the two above with device-resident input (a device pointer to H*W uint16) */
+/* same as the two above with device-resident input (a device pointer to H*W uint16),
+ * copied in the handle's stream order */
 kf_status kf_initial_processing_device(kf_handle* h, const uint16_t* depth_dev);
 kf_status kf_incoming_frame_device(kf_handle* h, const uint16_t* depth_dev);
 /* reads dep%04d.dat (system_utility.cpp:58-68) from dir into depth (H*W uint16) */
