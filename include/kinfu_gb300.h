@@ -122,7 +122,7 @@ kf_status kf_initial_processing(kf_handle* h, const uint16_t* depth);
  * every call reading images or the volume) waits for it, kf_get_pose for its pose. */
 kf_status kf_incoming_frame(kf_handle* h, const uint16_t* depth);
 /* same as the two above with device-resident input (a device pointer to H*W uint16),
- * copied in the handle's stream order */
+ * read in the handle's stream order (by kf_incoming_frame_device's graph in place) */
 kf_status kf_initial_processing_device(kf_handle* h, const uint16_t* depth_dev);
 kf_status kf_incoming_frame_device(kf_handle* h, const uint16_t* depth_dev);
 /* reads dep%04d.dat (system_utility.cpp:58-68) from dir into depth (H*W uint16) */

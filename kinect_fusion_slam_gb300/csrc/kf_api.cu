@@ -50,7 +50,11 @@ void destroy_graphs(kf_handle* h)
     if (h->g_incoming) cudaGraphExecDestroy(h->g_incoming);
     if (h->g_incoming_alt) cudaGraphExecDestroy(h->g_incoming_alt);
     if (h->g_initial) cudaGraphExecDestroy(h->g_initial);
-    h->g_incoming = h->g_incoming_alt = h->g_initial = nullptr;
+    if (h->g_incoming_dev) cudaGraphExecDestroy(h->g_incoming_dev);
+    if (h->g_dev_graph) cudaGraphDestroy(h->g_dev_graph);
+    h->g_incoming = h->g_incoming_alt = h->g_initial = h->g_incoming_dev = nullptr;
+    h->g_dev_graph = nullptr;
+    h->dev_node = nullptr;
 }
 
 bool validate(const kf_config* c, std::string& why)
@@ -749,15 +753,65 @@ kf_status kf_initial_processing_device(kf_handle* h, const uint16_t* depth_dev)
     return KF_OK;
 }
 
+// The incoming-frame graph for device-resident input: captured like g_incoming, with
+// the vertex kernel's node and arguments kept so that each frame points its raw input
+// at the caller's buffer (the graph then reads it in stream order, with no copy).
+kf_status capture_device_graph(kf_handle* h)
+{
+    KF_CUDA(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    enq_incoming(h, h->d_raw);
+    cudaError_t le = cudaGetLastError();
+    cudaGraph_t graph = nullptr;
+    cudaError_t ce = cudaStreamEndCapture(h->stream, &graph);
+    if (le != cudaSuccess || ce != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        return fail(h, KF_ERR_CUDA, std::string("graph capture failed: ") + cudaGetErrorString(le != cudaSuccess ? le : ce));
+    }
+    size_t n = 0;
+    cudaGraphGetNodes(graph, nullptr, &n);
+    std::vector<cudaGraphNode_t> nodes(n);
+    cudaGraphGetNodes(graph, nodes.data(), &n);
+    for (cudaGraphNode_t nd : nodes) {
+        cudaGraphNodeType t;
+        if (cudaGraphNodeGetType(nd, &t) != cudaSuccess || t != cudaGraphNodeTypeKernel) continue;
+        cudaKernelNodeParams p{};
+        if (cudaGraphKernelNodeGetParams(nd, &p) == cudaSuccess && p.func == vertex_raw_kernel_func()) {
+            h->dev_node = nd;
+            h->dev_params = p;
+            for (int i = 0; i < kVertexKernelArgs; ++i) h->dev_args[i] = p.kernelParams[i];
+            break;
+        }
+    }
+    cudaError_t ie = h->dev_node ? cudaGraphInstantiate(&h->g_incoming_dev, graph, 0) : cudaErrorInvalidValue;
+    if (ie != cudaSuccess) {
+        cudaGraphDestroy(graph);
+        h->dev_node = nullptr;
+        h->g_incoming_dev = nullptr;
+        return fail(h, KF_ERR_CUDA, std::string("device-input graph: ") + cudaGetErrorString(ie));
+    }
+    h->g_dev_graph = graph;  // the node handle stays valid while the graph lives
+    return KF_OK;
+}
+
 kf_status kf_incoming_frame_device(kf_handle* h, const uint16_t* depth_dev)
 {
     KF_HANDLE(h);
     if (!depth_dev) return fail(h, KF_ERR_INVALID_ARGUMENT, "null depth");
-    // in stream order: the caller may have produced the frame on this stream
-    KF_CUDA(h, cudaMemcpyAsync(h->d_raw, depth_dev, sizeof(uint16_t) * h->cam.H * h->cam.W, cudaMemcpyDeviceToDevice,
-                               h->stream));
-    KF_TRY(run_captured(h, h->g_incoming, true, h->d_raw));
-    raw_used(h, 0);
+    if (h->cfg.use_graphs) {
+        if (!h->g_incoming_dev) KF_TRY(capture_device_graph(h));
+        h->dev_raw = depth_dev;
+        h->dev_args[0] = &h->dev_raw;
+        cudaKernelNodeParams p = h->dev_params;
+        p.kernelParams = h->dev_args;
+        KF_CUDA(h, cudaGraphExecKernelNodeSetParams(h->g_incoming_dev, h->dev_node, &p));
+        KF_CUDA(h, cudaGraphLaunch(h->g_incoming_dev, h->stream));
+    } else {
+        // in stream order: the caller may have produced the frame on this stream
+        KF_CUDA(h, cudaMemcpyAsync(h->d_raw, depth_dev, sizeof(uint16_t) * h->cam.H * h->cam.W,
+                                   cudaMemcpyDeviceToDevice, h->stream));
+        KF_TRY(run_captured(h, h->g_incoming, true, h->d_raw));
+        raw_used(h, 0);
+    }
     h->frame_timed = h->timing;
     h->pose_call = h->calls;
     return KF_OK;

@@ -287,6 +287,8 @@ void launch_vertex(const uint16_t* raw, float* depth, float4* vmap, float4* nmap
                                                     compute_normals ? 1 : 0);
 }
 
+const void* vertex_raw_kernel_func() { return reinterpret_cast<const void*>(&vertex_kernel<true>); }
+
 void launch_bilateral(const float* depth, float* out, const float* spatial, int r, float sigma_r, int H, int W,
                       cudaStream_t s)
 {

@@ -83,6 +83,16 @@ struct kf_handle {
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t ev_copied = nullptr, ev_raw_free[2] = {};
     int raw_turn = 0;  // buffer of the latest pinned frame
+
+    // Device-resident frames run g_incoming_dev, whose vertex kernel reads the caller's
+    // buffer directly: dev_node is that kernel's node in g_dev_graph and dev_args its
+    // argument pointers, the first patched to dev_raw for each frame.
+    cudaGraph_t g_dev_graph = nullptr;
+    cudaGraphExec_t g_incoming_dev = nullptr;
+    cudaGraphNode_t dev_node = nullptr;
+    cudaKernelNodeParams dev_params{};
+    void* dev_args[16] = {};
+    const uint16_t* dev_raw = nullptr;
     mutable unsigned long long calls = 0;
     unsigned long long pose_call = 0;
 };

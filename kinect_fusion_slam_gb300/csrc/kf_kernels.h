@@ -16,6 +16,10 @@ void launch_fill_nan_half2(__half2* p, size_t n, cudaStream_t s);
 // depth ingest (+ inclusive range filter when raw != nullptr) fused with the
 // vertex/normal map of raw_vertices.cu:3-51.  With init_icp, thread 0 also prepares
 // the frame's ICP state (T_prev^-1 and F) from st->T.
+// the kernel launch_vertex runs on raw input (its first argument is the raw pointer,
+// of kVertexKernelArgs arguments), for patching a captured graph's input per frame
+constexpr int kVertexKernelArgs = 10;
+const void* vertex_raw_kernel_func();
 void launch_vertex(const uint16_t* raw, float* depth, float4* vmap, float4* nmap, const Camera& cam, float dmin,
                    float dmax, State* st, bool init_icp, bool compute_normals, cudaStream_t s);
 
