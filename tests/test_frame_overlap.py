@@ -14,19 +14,23 @@ import kinect_fusion_slam_gb300 as kf
 pytestmark = pytest.mark.gpu
 
 
-def _handle(seq, H, W):
+PRECISION = dict(tsdf_storage=kf.KF_TSDF_F16, solve_mode=kf.KF_SOLVE_PRECISE, icp_reduction=kf.KF_REDUCE_TREE)
+
+
+def _handle(seq, H, W, **extra):
     g = seq.cfg.grid
-    h = kf.Handle(kf.make_config(height=H, width=W, dims=g.dims, grid_start=g.start, voxel_size=g.voxel_size))
+    h = kf.Handle(
+        kf.make_config(height=H, width=W, dims=g.dims, grid_start=g.start, voxel_size=g.voxel_size, **extra))
     K = seq.K
     h.set_intrinsics(K[0, 0], K[1, 1], K[0, 2], K[1, 2])
     return h
 
 
-def _run(seq, depths, mode):
+def _run(seq, depths, mode, **extra):
     import torch
 
     H, W = depths.shape[1:]
-    h = _handle(seq, H, W)
+    h = _handle(seq, H, W, **extra)
     n = len(depths)
     fb = H * W * 2
     pinned = torch.from_numpy(depths.view(np.int16)).pin_memory()
@@ -48,14 +52,26 @@ def _run(seq, depths, mode):
     return poses, pred
 
 
-def test_pinned_pageable_and_device_frames_agree(small_seq):
+def _same(a, b):
+    return np.array_equal(np.asarray(a).view(np.uint32), np.asarray(b).view(np.uint32))
+
+
+@pytest.mark.parametrize("form", ["plain", "precision"])
+def test_pinned_pageable_and_device_frames_agree(small_seq, form):
+    """Every input path, with and without the per-frame CUDA graphs, against the graph
+    device-input run.  The precision form's sums are exact fixed-point accumulations, so
+    its results do not depend on the order the blocks finish in either."""
     seq, depths = small_seq
     depths = np.concatenate([depths, depths[::-1][1:]])  # 7 frames: forwards and back
-    ref_poses, ref_pred = _run(seq, depths, "device")
-    for mode in ("pinned", "pageable", "pinned_interleaved"):
-        poses, pred = _run(seq, depths, mode)
-        assert all(np.array_equal(a.view(np.uint32), b.view(np.uint32)) for a, b in zip(poses, ref_poses)), mode
-        assert np.array_equal(pred.view(np.uint32), ref_pred.view(np.uint32)), mode
-    poses, pred = _run(seq, depths, "pinned_ahead")
-    assert np.array_equal(poses[-1].view(np.uint32), ref_poses[-1].view(np.uint32))
-    assert np.array_equal(pred.view(np.uint32), ref_pred.view(np.uint32))
+    extra = PRECISION if form == "precision" else {}
+    ref_poses, ref_pred = _run(seq, depths, "device", **extra)
+    for graphs in (1, 0):
+        for mode in ("device", "pinned", "pageable", "pinned_interleaved"):
+            if graphs and mode == "device":
+                continue
+            poses, pred = _run(seq, depths, mode, use_graphs=graphs, **extra)
+            assert all(_same(a, b) for a, b in zip(poses, ref_poses)), (mode, graphs)
+            assert _same(pred, ref_pred), (mode, graphs)
+        poses, pred = _run(seq, depths, "pinned_ahead", use_graphs=graphs, **extra)
+        assert _same(poses[-1], ref_poses[-1]), graphs
+        assert _same(pred, ref_pred), graphs
