@@ -55,6 +55,10 @@ struct ViewF32 {
     __device__ __forceinline__ float value(int i) const { return __ldg(t + i); }
     __device__ __forceinline__ Raw raw(int i) const { return __ldg(t + i); }
     __device__ static __forceinline__ float decode(Raw r) { return r; }
+    // below kNegativeKeys exactly for a value < 0 (not -0, not NaN): bits in
+    // [0x80000001, 0xff800000]
+    __device__ static __forceinline__ unsigned negative_key(Raw r) { return __float_as_uint(r) - 0x80000001u; }
+    static constexpr unsigned kNegativeKeys = 0x7f800000u;
 };
 
 struct ViewF16 {
@@ -66,6 +70,10 @@ struct ViewF16 {
     {
         return __half2float(__ushort_as_half((unsigned short)(r & 0xffffu)));
     }
+    // below kNegativeKeys exactly for a value < 0 (not -0, not NaN): the value's bits in
+    // [0x8001, 0xfc00], moved to the top half (the weight's bits drop out)
+    __device__ static __forceinline__ unsigned negative_key(Raw r) { return (r << 16) - 0x80010000u; }
+    static constexpr unsigned kNegativeKeys = 0x7c000000u;
 };
 
 // Per pixel (u, v) (1-based): the quantities of projective_tsdf.cu:39-95 that depend
@@ -598,13 +606,16 @@ __device__ __forceinline__ void trace(const View& vol, float X, float Y, float D
 
     bool inside = false;
     float tmin = slab_entry(inside, dir, lo, hi, org);
-    if (!inside) return;
+    // every lane of the warp walks (the group votes below take the full mask); a lane
+    // without a ray (no depth, or a ray that misses the grid) starts finished
+    const bool walks = D != 0 && inside;
     if (tmin < 0) tmin = 0;
     const float3 s = make_float3(org.x + tmin * dir.x, org.y + tmin * dir.y, org.z + tmin * dir.z);
     const float3 box = make_float3(hi.x - lo.x, hi.y - lo.y, hi.z - lo.z);
     int ix = (int)floorf(((s.x - lo.x) / box.x) * L) + 1;
     int iy = (int)floorf(((s.y - lo.y) / box.y) * Wd) + 1;
     int iz = (int)floorf(((s.z - lo.z) / box.z) * Hz) + 1;
+    if (!walks) ix = iy = iz = 1;
     if (ix == L + 1) ix = ix - 1;
     if (iy == Wd + 1) iy = iy - 1;
     if (iz == Hz + 1) iz = iz - 1;
@@ -651,7 +662,7 @@ __device__ __forceinline__ void trace(const View& vol, float X, float Y, float D
     // inside iff the steps each axis has left before that side, r = (n - 2) - i going up
     // or i - 1 going down, are all >= 0 -- one OR and one sign test per position, and
     // once outside a walk stays outside.
-    const bool start_in = inside_grid(ix, iy, iz);
+    const bool start_in = walks && inside_grid(ix, iy, iz);
     int rx = sx > 0 ? (L - 2) - ix : ix - 1;
     int ry = sy > 0 ? (Wd - 2) - iy : iy - 1;
     int rz = sz > 0 ? (Hz - 2) - iz : iz - 1;
@@ -659,13 +670,14 @@ __device__ __forceinline__ void trace(const View& vol, float X, float Y, float D
     // The stepping never depends on the loaded values, only the termination does, so a
     // lead walker with the same arithmetic runs kAhead steps in front: at each position
     // it issues the voxel's load into a register ring and records, beside it, the
-    // position's linear index, whether it is inside the bounds and which axis the step
-    // from it takes (the Amanatides-Woo step, :384-417: the same three comparisons pick
-    // the axis).  The trailing walk consumes value, index, flag and axis in order and
-    // keeps no indices of its own.  The reference's XY..ZY (the other two indices at the
-    // last step along x, y, z) are kept as the linear index of the position each last
-    // such step left from (-1 before the first: the reference's never-assigned zeros)
-    // and decoded after the walk.  The lead loads only voxels inside the bounds.
+    // position's linear index and a code, the one-hot axis of the step from it (the
+    // Amanatides-Woo step, :384-417: the same three comparisons pick the axis) when the
+    // position is inside the bounds, else 0.  The trailing walk consumes value, index and
+    // code in order and keeps no indices of its own.  The reference's XY..ZY (the other
+    // two indices at the last step along x, y, z) are kept as the linear index of the
+    // position each last such step left from (-1 before the first: the reference's
+    // never-assigned zeros) and decoded after the walk.  The lead loads only voxels
+    // inside the bounds.
     constexpr int kAhead = 4;
     int ali = li;
     float3 atm = tm;
@@ -676,65 +688,105 @@ __device__ __forceinline__ void trace(const View& vol, float X, float Y, float D
             rx -= 1;
             ali += dlx;
             atm.x = atm.x + td.x;
-            axis = 0;
+            axis = 1;
         } else if (!xy && yz) {
             ry -= 1;
             ali += dly;
             atm.y = atm.y + td.y;
-            axis = 1;
+            axis = 2;
         } else {
             rz -= 1;
             ali += dlz;
             atm.z = atm.z + td.z;
-            axis = 2;
+            axis = 4;
         }
         return axis;
     };
     typename View::Raw ring[kAhead];
     int ring_li[kAhead];
-    int code[kAhead];  // 4: inside the bounds, | axis of the step
+    int code[kAhead];
 #pragma unroll
     for (int k = 0; k < kAhead; ++k) {
         const bool in = (rx | ry | rz) >= 0;
         ring[k] = in ? vol.raw(ali) : typename View::Raw(0);
         ring_li[k] = ali;
-        code[k] = (in ? 4 : 0) | lead_step();
+        const int axis = lead_step();
+        code[k] = in ? axis : 0;
     }
     float prev = 0.0f;
     float crossing = 0.f;  // the negative value met right after a positive one, or 0
     int rec_x = -1, rec_y = -1, rec_z = -1;
-    bool done = false;
-    // Steps run in groups of kAhead without branches: a lane whose walk has ended keeps
-    // stepping with its results frozen until the group ends, and the loop is left
-    // between groups.  Every step moves one index one step in a fixed direction, so
-    // the walk ends within L + Wd + Hz steps; the bound only makes that explicit.
+    bool done = !start_in;
+    // Steps run in groups of kAhead without branches; the warp leaves the loop when
+    // every lane's walk has ended, and a lane whose walk has ended steps on with its
+    // results frozen and its lead outside the bounds (no loads).  Every step moves one
+    // index one step in a fixed direction, so a walk ends within L + Wd + Hz steps; the
+    // bound only makes that explicit.
     for (int guard = 0; guard < L + Wd + Hz + 4; guard += kAhead) {
+        // A group in which every walking lane has kAhead positions inside the bounds, none
+        // of negative value, after a previous value that is not negative, advances through
+        // all of them by the reference's tests: each of :207-222 needs a negative value
+        // before or at the position, and so does a zero crossing.  When the whole warp is
+        // in that case, only the lead and the axis records run.
+        unsigned key = View::negative_key(ring[0]);
+        bool all_in = code[0] != 0;
 #pragma unroll
-        for (int k = 0; k < kAhead; ++k) {
-            const int c = code[k];
-            const float cur = View::decode(ring[k]);
-            const int here = ring_li[k];
-            const bool in = (rx | ry | rz) >= 0;
-            ring[k] = in ? vol.raw(ali) : typename View::Raw(0);
-            ring_li[k] = ali;
-            code[k] = (in ? 4 : 0) | lead_step();
-            // the position ends the walk if it is outside the bounds, or by the
-            // reference's four tests (:207-222, mutually exclusive in prev), or as the
-            // zero crossing (a negative value right after a positive one)
-            const bool live = !done && (c & 4);
-            const bool stop = prev < 0.f ? !(cur <= 0.f) : (isnan(prev) && cur < 0.f);
-            const bool cross = live && !stop && prev > 0.f && cur < 0.f;
-            crossing = cross ? cur : crossing;
-            li = cross ? here : li;
-            const bool adv = live && !stop && !cross;
-            done = !adv;
-            prev = adv ? cur : prev;
-            const int axis = c & 3;
-            rec_x = (adv && axis == 0) ? here : rec_x;
-            rec_y = (adv && axis == 1) ? here : rec_y;
-            rec_z = (adv && axis == 2) ? here : rec_z;
+        for (int k = 1; k < kAhead; ++k) {
+            key = min(key, View::negative_key(ring[k]));
+            all_in = all_in && code[k] != 0;
         }
-        if (done) break;
+        const bool easy = done || (!(prev < 0.f) && all_in && key >= View::kNegativeKeys);
+        if (__all_sync(0xffffffffu, easy)) {
+            const typename View::Raw last = ring[kAhead - 1];
+#pragma unroll
+            for (int k = 0; k < kAhead; ++k) {
+                const int c = code[k];  // 0 for a finished lane: no records change
+                const int here = ring_li[k];
+                const bool in = (rx | ry | rz) >= 0;
+                ring[k] = in ? vol.raw(ali) : typename View::Raw(0);
+                ring_li[k] = ali;
+                const int axis = lead_step();
+                code[k] = in ? axis : 0;
+                rec_x = (c & 1) ? here : rec_x;
+                rec_y = (c & 2) ? here : rec_y;
+                rec_z = (c & 4) ? here : rec_z;
+            }
+            prev = View::decode(last);  // unused once the walk has ended
+        } else {
+#pragma unroll
+            for (int k = 0; k < kAhead; ++k) {
+                const int c = code[k];
+                const float cur = View::decode(ring[k]);
+                const int here = ring_li[k];
+                const bool in = (rx | ry | rz) >= 0;
+                ring[k] = in ? vol.raw(ali) : typename View::Raw(0);
+                ring_li[k] = ali;
+                const int axis = lead_step();
+                code[k] = in ? axis : 0;
+                // the position ends the walk if it is outside the bounds, or by the
+                // reference's four tests (:207-222, mutually exclusive in prev), or as
+                // the zero crossing (a negative value right after a positive one)
+                const bool live = !done && c != 0;
+                const bool stop = prev < 0.f ? !(cur <= 0.f) : (isnan(prev) && cur < 0.f);
+                const bool cross = live && !stop && prev > 0.f && cur < 0.f;
+                crossing = cross ? cur : crossing;
+                li = cross ? here : li;
+                const bool adv = live && !stop && !cross;
+                done = !adv;
+                prev = adv ? cur : prev;
+                rec_x = (adv && (c & 1)) ? here : rec_x;
+                rec_y = (adv && (c & 2)) ? here : rec_y;
+                rec_z = (adv && (c & 4)) ? here : rec_z;
+            }
+            if (done) {
+                // the lead's positions queued behind the end carry no records, and it
+                // issues no further loads
+#pragma unroll
+                for (int k = 0; k < kAhead; ++k) code[k] = 0;
+                rx = -1;
+            }
+        }
+        if (__all_sync(0xffffffffu, done)) break;
     }
     if (!(crossing < 0.f)) return;
     // the crossing's position and the recorded indices, 1-based as in the reference
@@ -846,12 +898,14 @@ __global__ void __launch_bounds__(kRayBlock, 4) raycast_kernel(View vol, const f
         }
         const int px = (int)(tile % tiles_x) * 8 + (lane & 7);
         const int py = (int)(tile / tiles_x) * 4 + (lane >> 3);
-        if (px >= cam.W || py >= cam.H) continue;
+        // every lane traces (a lane off the image or without depth walks no steps)
+        const bool pixel = px < cam.W && py < cam.H;
         const int i = py * cam.W + px;
         float4 op = make_float4(0.f, 0.f, 0.f, 0.f), on = op;
         int oh = -1;
-        const float D = depth[i];
-        if (D != 0) trace(vol, (float)px + 1.0f, (float)py + 1.0f, D, cam.Ki, T, g, c_flip, op, on, oh);
+        const float D = pixel ? depth[i] : 0.f;
+        trace(vol, (float)px + 1.0f, (float)py + 1.0f, D, cam.Ki, T, g, c_flip, op, on, oh);
+        if (!pixel) continue;
         pv[i] = op;
         pn[i] = on;
         if (hit) hit[i] = oh;
@@ -893,17 +947,17 @@ __global__ void __launch_bounds__(kRayBlock, 4) raycast_batch_kernel(const Scene
         const int tiles_x = (cam.W + TW - 1) / TW;
         const int px = (int)(t % tiles_x) * TW + (lane % TW);
         const int py = (int)(t / tiles_x) * TH + lane / TW;
-        if (px >= cam.W || py >= cam.H) continue;
+        const bool pixel = px < cam.W && py < cam.H;
         float T[12];
 #pragma unroll
         for (int k = 0; k < 12; ++k) T[k] = d.st->T[k];
         const int i = py * cam.W + px;
         float4 op = make_float4(0.f, 0.f, 0.f, 0.f), on = op;
         int oh = -1;
-        const float D = d.depth[0][i];
-        if (D != 0)
-            trace(scene_view(d, (View*)nullptr), (float)px + 1.0f, (float)py + 1.0f, D, cam.Ki, T, d.grid,
-                  d.st->c_flip, op, on, oh);
+        const float D = pixel ? d.depth[0][i] : 0.f;
+        trace(scene_view(d, (View*)nullptr), (float)px + 1.0f, (float)py + 1.0f, D, cam.Ki, T, d.grid, d.st->c_flip,
+              op, on, oh);
+        if (!pixel) continue;
         d.pv[0][i] = op;
         d.pn[0][i] = on;
         if (d.hit) d.hit[i] = oh;
