@@ -670,37 +670,36 @@ __device__ __forceinline__ void trace(const View& vol, float X, float Y, float D
     // The stepping never depends on the loaded values, only the termination does, so a
     // lead walker with the same arithmetic runs kAhead steps in front: at each position
     // it issues the voxel's load into a register ring and records, beside it, the
-    // position's linear index and a code, the one-hot axis of the step from it (the
-    // Amanatides-Woo step, :384-417: the same three comparisons pick the axis) when the
-    // position is inside the bounds, else 0.  The trailing walk consumes value, index and
-    // code in order and keeps no indices of its own.  The reference's XY..ZY (the other
-    // two indices at the last step along x, y, z) are kept as the linear index of the
-    // position each last such step left from (-1 before the first: the reference's
-    // never-assigned zeros) and decoded after the walk.  The lead loads only voxels
-    // inside the bounds.
+    // position's linear index and a code, the linear-index delta of the step from it
+    // (the Amanatides-Woo step, :384-417: the same three comparisons pick the axis;
+    // dlx, dly, dlz are distinct and nonzero since every side is at least 3 voxels) when
+    // the position is inside the bounds, else 0.  The trailing walk consumes value,
+    // index and code in order and keeps no indices of its own.  The reference's XY..ZY
+    // (the other two indices at the last step along x, y, z) are kept as the linear
+    // index of the position each last such step left from (-1 before the first: the
+    // reference's never-assigned zeros) and decoded after the walk.  The lead loads only
+    // voxels inside the bounds.
     constexpr int kAhead = 4;
     int ali = li;
     float3 atm = tm;
     auto lead_step = [&]() -> int {
         const bool xy = atm.x < atm.y, xz = atm.x < atm.z, yz = atm.y < atm.z;
-        int axis;
+        int d;
         if (xy && xz) {
             rx -= 1;
-            ali += dlx;
             atm.x = atm.x + td.x;
-            axis = 1;
+            d = dlx;
         } else if (!xy && yz) {
             ry -= 1;
-            ali += dly;
             atm.y = atm.y + td.y;
-            axis = 2;
+            d = dly;
         } else {
             rz -= 1;
-            ali += dlz;
             atm.z = atm.z + td.z;
-            axis = 4;
+            d = dlz;
         }
-        return axis;
+        ali += d;
+        return d;
     };
     typename View::Raw ring[kAhead];
     int ring_li[kAhead];
@@ -710,8 +709,8 @@ __device__ __forceinline__ void trace(const View& vol, float X, float Y, float D
         const bool in = (rx | ry | rz) >= 0;
         ring[k] = in ? vol.raw(ali) : typename View::Raw(0);
         ring_li[k] = ali;
-        const int axis = lead_step();
-        code[k] = in ? axis : 0;
+        const int step = lead_step();
+        code[k] = in ? step : 0;
     }
     float prev = 0.0f;
     float crossing = 0.f;  // the negative value met right after a positive one, or 0
@@ -743,13 +742,13 @@ __device__ __forceinline__ void trace(const View& vol, float X, float Y, float D
                 const int c = code[k];  // 0 for a finished lane: no records change
                 const int here = ring_li[k];
                 const bool in = (rx | ry | rz) >= 0;
-                ring[k] = in ? vol.raw(ali) : typename View::Raw(0);
+                if (in) ring[k] = vol.raw(ali);  // outside the bounds: a stale value, unused (code 0)
                 ring_li[k] = ali;
-                const int axis = lead_step();
-                code[k] = in ? axis : 0;
-                rec_x = (c & 1) ? here : rec_x;
-                rec_y = (c & 2) ? here : rec_y;
-                rec_z = (c & 4) ? here : rec_z;
+                const int step = lead_step();
+                code[k] = in ? step : 0;
+                rec_x = c == dlx ? here : rec_x;
+                rec_y = c == dly ? here : rec_y;
+                rec_z = c == dlz ? here : rec_z;
             }
             prev = View::decode(last);  // unused once the walk has ended
         } else {
@@ -759,10 +758,10 @@ __device__ __forceinline__ void trace(const View& vol, float X, float Y, float D
                 const float cur = View::decode(ring[k]);
                 const int here = ring_li[k];
                 const bool in = (rx | ry | rz) >= 0;
-                ring[k] = in ? vol.raw(ali) : typename View::Raw(0);
+                if (in) ring[k] = vol.raw(ali);
                 ring_li[k] = ali;
-                const int axis = lead_step();
-                code[k] = in ? axis : 0;
+                const int step = lead_step();
+                code[k] = in ? step : 0;
                 // the position ends the walk if it is outside the bounds, or by the
                 // reference's four tests (:207-222, mutually exclusive in prev), or as
                 // the zero crossing (a negative value right after a positive one)
@@ -774,9 +773,9 @@ __device__ __forceinline__ void trace(const View& vol, float X, float Y, float D
                 const bool adv = live && !stop && !cross;
                 done = !adv;
                 prev = adv ? cur : prev;
-                rec_x = (adv && (c & 1)) ? here : rec_x;
-                rec_y = (adv && (c & 2)) ? here : rec_y;
-                rec_z = (adv && (c & 4)) ? here : rec_z;
+                rec_x = (adv && c == dlx) ? here : rec_x;
+                rec_y = (adv && c == dly) ? here : rec_y;
+                rec_z = (adv && c == dlz) ? here : rec_z;
             }
             if (done) {
                 // the lead's positions queued behind the end carry no records, and it
