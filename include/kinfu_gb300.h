@@ -97,6 +97,9 @@ kf_status kf_get_config(const kf_handle* h, kf_config* cfg);
 
 /* intrinsic_matrix (kinfu_pipeline.h:17): fx, fy and the 1-based principal point */
 kf_status kf_set_intrinsics(kf_handle* h, float fx, float fy, float cx, float cy);
+/* the same with the principal point's convention chosen: one_based != 0 as above;
+ * one_based == 0 takes a 0-based (cx, cy), stored as (cx + 1, cy + 1) in float */
+kf_status kf_set_intrinsics_ex(kf_handle* h, float fx, float fy, float cx, float cy, int one_based);
 kf_status kf_get_intrinsics(const kf_handle* h, float K[9]);
 /* extrinsic_matrix (kinfu_pipeline.h:18): 4x4 row-major camera-to-world, mm */
 kf_status kf_set_pose(kf_handle* h, const float T[16]);
@@ -121,6 +124,8 @@ kf_status kf_initial_processing(kf_handle* h, const uint16_t* depth);
  * integration, ray cast.  Asynchronous on the handle's stream; kf_synchronize (and
  * every call reading images or the volume) waits for it, kf_get_pose for its pose. */
 kf_status kf_incoming_frame(kf_handle* h, const uint16_t* depth);
+/* one call for both: is_first != 0 is kf_initial_processing, else kf_incoming_frame */
+kf_status kf_process_frame(kf_handle* h, const uint16_t* depth, int is_first);
 /* same as the two above with device-resident input (a device pointer to H*W uint16),
  * read in the handle's stream order (by kf_incoming_frame_device's graph in place) */
 kf_status kf_initial_processing_device(kf_handle* h, const uint16_t* depth_dev);

@@ -111,8 +111,10 @@ class Handle:
         return d
 
     # -- camera and pose ------------------------------------------------------------
-    def set_intrinsics(self, fx, fy, cx, cy) -> None:
-        self._check(self.lib.kf_set_intrinsics(self.h, fx, fy, cx, cy))
+    def set_intrinsics(self, fx, fy, cx, cy, one_based: bool = True) -> None:
+        """fx, fy and the principal point: 1-based (the reference's K) unless one_based
+        is False"""
+        self._check(self.lib.kf_set_intrinsics_ex(self.h, fx, fy, cx, cy, int(one_based)))
 
     def intrinsics(self) -> np.ndarray:
         K = np.zeros(9, np.float32)
@@ -138,6 +140,11 @@ class Handle:
     def incoming_frame(self, depth_u16) -> None:
         d = self._u16(depth_u16)
         self._check(self.lib.kf_incoming_frame(self.h, _lib.ptr(d)))
+
+    def process_frame(self, depth_u16, is_first: bool) -> None:
+        """initial_processing when is_first, else incoming_frame (kf_process_frame)"""
+        d = self._u16(depth_u16)
+        self._check(self.lib.kf_process_frame(self.h, _lib.ptr(d), int(is_first)))
 
     def initial_processing_ptr(self, host_ptr: int) -> None:
         """host_ptr: address of H*W uint16 (pinned host memory avoids a staging copy)"""

@@ -92,12 +92,14 @@ SIGNATURES = {
     "kf_status_string": (C.c_char_p, [C.c_int]),
     "kf_get_config": (C.c_int, [_H, C.POINTER(Config)]),
     "kf_set_intrinsics": (C.c_int, [_H, C.c_float, C.c_float, C.c_float, C.c_float]),
+    "kf_set_intrinsics_ex": (C.c_int, [_H, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int]),
     "kf_get_intrinsics": (C.c_int, [_H, _f32p]),
     "kf_set_pose": (C.c_int, [_H, _f32p]),
     "kf_get_pose": (C.c_int, [_H, _f32p]),
     "kf_reset": (C.c_int, [_H]),
     "kf_initial_processing": (C.c_int, [_H, _vp]),
     "kf_incoming_frame": (C.c_int, [_H, _vp]),
+    "kf_process_frame": (C.c_int, [_H, _vp, C.c_int]),
     "kf_initial_processing_device": (C.c_int, [_H, _vp]),
     "kf_incoming_frame_device": (C.c_int, [_H, _vp]),
     "kf_load_depth_dat": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_int, _u16p]),

@@ -633,6 +633,11 @@ kf_status kf_set_intrinsics(kf_handle* h, float fx, float fy, float cx, float cy
     return KF_OK;
 }
 
+kf_status kf_set_intrinsics_ex(kf_handle* h, float fx, float fy, float cx, float cy, int one_based)
+{
+    return one_based ? kf_set_intrinsics(h, fx, fy, cx, cy) : kf_set_intrinsics(h, fx, fy, cx + 1.f, cy + 1.f);
+}
+
 kf_status kf_get_intrinsics(const kf_handle* h, float K[9])
 {
     if (!h || !K) return KF_ERR_INVALID_ARGUMENT;
@@ -739,6 +744,11 @@ kf_status kf_incoming_frame(kf_handle* h, const uint16_t* depth)
     h->frame_timed = h->timing;
     h->pose_call = h->calls;
     return KF_OK;
+}
+
+kf_status kf_process_frame(kf_handle* h, const uint16_t* depth, int is_first)
+{
+    return is_first ? kf_initial_processing(h, depth) : kf_incoming_frame(h, depth);
 }
 
 kf_status kf_initial_processing_device(kf_handle* h, const uint16_t* depth_dev)

@@ -581,6 +581,8 @@ __device__ __forceinline__ float slab_entry(bool& inside, float3 d, float3 lo, f
 // One ray of Voxel_Traversal (voxel_traversal.cu:90-422).  The axis records XY..ZY
 // start at 0, so a zero crossing met before the ray has stepped along every axis is
 // not a hit (the reference leaves them uninitialised; zero is what g++ -O2 gives).
+// Called by all 32 lanes of a warp together (the walk's votes take the full mask); a
+// lane without a ray passes D = 0.
 template <class View>
 __device__ __forceinline__ void trace(const View& vol, float X, float Y, float D, const float* Ki, const float* T,
                                       const Grid& g, float c_flip, float4& op, float4& on, int& oh)

@@ -449,6 +449,27 @@ def test_graph_and_eager_agree(small_seq):
     assert np.array_equal(poses[0], poses[1])
 
 
+def test_process_frame_and_zero_based_intrinsics(small_seq):
+    """kf_process_frame(is_first) is kf_initial_processing / kf_incoming_frame, and a
+    0-based principal point through kf_set_intrinsics_ex gives the reference's K."""
+    seq, depths = small_seq
+    a = make_handle(seq)
+    g = seq.cfg.grid
+    b = kf.Handle(kf.make_config(height=a.H, width=a.W, dims=g.dims, grid_start=g.start, voxel_size=g.voxel_size))
+    K = seq.K
+    b.set_intrinsics(K[0, 0], K[1, 1], np.float32(K[0, 2] - 1), np.float32(K[1, 2] - 1), one_based=False)
+    assert np.array_equal(a.intrinsics(), b.intrinsics())
+    a.initial_processing(depths[0])
+    b.process_frame(depths[0], is_first=True)
+    for k in range(1, len(depths)):
+        a.incoming_frame(depths[k])
+        b.process_frame(depths[k], is_first=False)
+        assert np.array_equal(a.pose().view(np.uint32), b.pose().view(np.uint32)), k
+    assert np.array_equal(a.predicted().view(np.uint32), b.predicted().view(np.uint32))
+    a.close()
+    b.close()
+
+
 def test_invalid_arguments(small_seq):
     seq, _ = small_seq
     h = make_handle(seq)
