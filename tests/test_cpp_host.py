@@ -3,8 +3,8 @@ SystemUtility interface over the C ABI) and the headless frame loop built on it
 (kinect_fusion_slam_gb300/driver/kinfu_run.cpp, the reference's system_interface.cpp
 without the viewer).
 
-On the CPU: the header compiles on its own and the driver is built and rejects bad
-arguments.  On the GPU: the driver, reading dep%04d.dat frames as the reference does,
+On the CPU: the header compiles on its own and kinfu_run is built and rejects bad
+arguments.  On the GPU: kinfu_run, reading dep%04d.dat frames as the reference does,
 produces the same poses, bit for bit, as the Python binding driving the same library
 on the same frames, in both forms."""
 import shutil
@@ -36,7 +36,7 @@ def test_header_compiles_alone(tmp_path):
     assert r.returncode == 0, r.stderr
 
 
-def test_driver_rejects_bad_arguments():
+def test_kinfu_run_rejects_bad_arguments():
     drv = _built()
     r = subprocess.run([str(drv), "--bogus"], capture_output=True, text=True)
     assert r.returncode == 2 and "usage" in r.stderr
@@ -51,7 +51,7 @@ def _write_frames(d: Path, depths, first: int):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("precision", [False, True])
-def test_driver_poses_match_python_binding(tmp_path, precision):
+def test_kinfu_run_poses_match_python_binding(tmp_path, precision):
     import kinect_fusion_slam_gb300 as kf
     from kinect_fusion_slam_gb300 import scene
 
