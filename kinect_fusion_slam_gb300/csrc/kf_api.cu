@@ -574,7 +574,8 @@ kf_status kf_create(const kf_config* cfg, kf_handle** out)
     h->cfg = *cfg;
     cudaGetDevice(&h->device);
     h->grid = Grid{cfg->dims[0], cfg->dims[1], cfg->dims[2], cfg->grid_start[0], cfg->grid_start[1],
-                   cfg->grid_start[2], cfg->voxel_size, cfg->truncated_distance, cfg->sdf_minimum, cfg->sdf_maximum};
+                   cfg->grid_start[2], cfg->voxel_size, cfg->truncated_distance, cfg->sdf_minimum, cfg->sdf_maximum,
+                   div_magic((uint32_t)cfg->dims[0]), div_magic((uint32_t)cfg->dims[1])};
     h->cam.H = cfg->height;
     h->cam.W = cfg->width;
     // the reference's intrinsics (kinfu_pipeline.cpp:14-24)

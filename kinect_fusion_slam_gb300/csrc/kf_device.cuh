@@ -5,6 +5,7 @@
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
+#include "kf_divmagic.h"
 #include "kf_math.cuh"
 
 namespace kf {
@@ -20,6 +21,7 @@ struct Grid {
     int sx, sy, sz;  // integer voxel coordinate of voxel (0,0,0)
     float vd;        // voxel size, mm
     float trunc, sdf_min, sdf_max;
+    DivMagic qdx, qdy;  // division by dx and by dy (decoding linear indices)
 };
 
 struct Camera {

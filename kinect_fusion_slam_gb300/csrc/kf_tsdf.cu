@@ -791,27 +791,28 @@ __device__ __forceinline__ void trace(const View& vol, float X, float Y, float D
     }
     if (!(crossing < 0.f)) return;
     // the crossing's position and the recorded indices, 1-based as in the reference
+    // (linear indices are non-negative and below 2^31; the divisions are multiply-highs)
     {
-        const int q = li / L;
+        const int q = div_by(li, g.qdx), r = div_by(q, g.qdy);
         ix = li - q * L + 1;
-        iy = q % Wd + 1;
-        iz = q / Wd + 1;
+        iy = q - r * Wd + 1;
+        iz = r + 1;
     }
     int XY = 0, XZ = 0, YX = 0, YZ = 0, ZX = 0, ZY = 0;
     if (rec_x >= 0) {
-        const int q = rec_x / L;
-        XY = q % Wd + 1;
-        XZ = q / Wd + 1;
+        const int q = div_by(rec_x, g.qdx), r = div_by(q, g.qdy);
+        XY = q - r * Wd + 1;
+        XZ = r + 1;
     }
     if (rec_y >= 0) {
-        const int q = rec_y / L;
+        const int q = div_by(rec_y, g.qdx);
         YX = rec_y - q * L + 1;
-        YZ = q / Wd + 1;
+        YZ = div_by(q, g.qdy) + 1;
     }
     if (rec_z >= 0) {
-        const int q = rec_z / L;
+        const int q = div_by(rec_z, g.qdx);
         ZX = rec_z - q * L + 1;
-        ZY = q % Wd + 1;
+        ZY = q - div_by(q, g.qdy) * Wd + 1;
     }
     const float cur = crossing;
     const int xn = (ix - 1) - 1, xp = (ix - 1) + 1;
