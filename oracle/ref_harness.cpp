@@ -177,7 +177,9 @@ int kfr_icp_associate(int H, int W, const float* K, const float* F, const float*
         const float* plane = k < 6 ? right.data() + k * HW : left.data() + (k - 6) * HW;
         for (int b = 0; b < nblocks; ++b) {
             float s[64];
-            for (int t = 0; t < 64; ++t) s[t] = plane[b * 64 + t];
+            /* a last, partial block is padded with zeros, as the oracle does (the
+             * reference runs 640x480 = 4800 full blocks only) */
+            for (int t = 0; t < 64; ++t) s[t] = (long)b * 64 + t < HW ? plane[b * 64 + t] : 0.f;
             for (int st = 32; st > 0; st >>= 1)
                 for (int t = 0; t < st; ++t) s[t] += s[t + st];
             part[b] = s[0];
