@@ -201,8 +201,10 @@ kf_status kf_get_flip_threshold(kf_handle* h, float* c_flip);
  *   sums28: device, receives the 6 entries of A^T b, the 21 of the upper triangle of
  *           A^T A row by row, and the correspondence count (as a float);
  *   pair:   device H*W int32 (matched pixel index or -1), or NULL;
- *   stream: cudaStream_t passed as void* (NULL = the default stream).
- * Asynchronous on stream.  The first call on each device looks up the scratch array's
+ *   stream: cudaStream_t passed as void* (NULL = the default stream); it must belong
+ *           to the current device, else KF_ERR_INVALID_ARGUMENT.
+ * Asynchronous on stream.  A reduction whose bounded wait gave up writes NaN into all
+ * 28 entries of sums28.  The first call on each device looks up the scratch array's
  * device address (cudaGetSymbolAddress), so make that first call before any stream
  * capture.  All calls share the scratch array: calls that overlap on the GPU race. */
 kf_status kf_icp_associate_noalloc(int height, int width, const float K[9], const float F[16], const float T[16],
@@ -304,7 +306,15 @@ kf_status kf_get_stage_times(kf_handle* h, float ms[5]);
 kf_status kf_kernels_per_frame(kf_handle* h, int* n);
 
 /* ---- diagnostics (no counterpart in the reference) --------------------------------
- * The ICP pose update computes cv::Cholesky's and cv::Mat's double-accumulated results
+ * The polls each of the handle's bounded device waits makes before it gives up, sets
+ * the handle's error flag and returns (leaving that ICP iteration's pose unchanged;
+ * kf_get_pose then reports KF_ERR_CUDA).  polls >= 0 sets the limit (0: every bounded
+ * wait gives up at once -- a host-side way to exercise that error path without a GPU
+ * fault); polls < 0 restores the default (2^26 polls, about a second).  Kept across
+ * kf_reset.  The reference has no bounded waits (sensor_pose_estimation.cu:399 ignores
+ * every failure).  Synchronous. */
+kf_status kf_set_wait_limit(kf_handle* h, long long polls);
+/* The ICP pose update computes cv::Cholesky's and cv::Mat's double-accumulated results
  * in float-float arithmetic with an exact FP64 fallback.  This runs that code and its
  * FP64 restatement on seeded random 6x6 systems and 4x4 products (blocks x 4 warps x
  * systems_per_warp of each) on the current device and counts: [0] systems, [1] solves

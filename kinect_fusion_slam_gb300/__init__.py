@@ -20,8 +20,9 @@ from pathlib import Path
 import numpy as np
 
 from . import _lib
-from ._lib import (KF_ICP_FAIL_IDENTITY, KF_ICP_FAIL_REFERENCE, KF_REDUCE_REFERENCE_ORDER, KF_REDUCE_TREE,
-                   KF_SOLVE_PRECISE, KF_SOLVE_REFERENCE, KF_TSDF_F16, KF_TSDF_F32, Config, KinfuError)
+from ._lib import (KF_ERR_CUDA, KF_ERR_INVALID_ARGUMENT, KF_ERR_IO, KF_ERR_OUT_OF_MEMORY, KF_ERR_STATE,
+                   KF_ERR_UNSUPPORTED, KF_ICP_FAIL_IDENTITY, KF_ICP_FAIL_REFERENCE, KF_OK, KF_REDUCE_REFERENCE_ORDER,
+                   KF_REDUCE_TREE, KF_SOLVE_PRECISE, KF_SOLVE_REFERENCE, KF_TSDF_F16, KF_TSDF_F32, Config, KinfuError)
 
 __all__ = ["KinfuPipeline", "Handle", "Batch", "Config", "KinfuError", "make_config", "KF_TSDF_F32", "KF_TSDF_F16",
            "KF_ICP_FAIL_REFERENCE", "KF_ICP_FAIL_IDENTITY", "KF_SOLVE_REFERENCE", "KF_SOLVE_PRECISE",
@@ -269,6 +270,11 @@ class Handle:
         ms = np.zeros(5, np.float32)
         self._check(self.lib.kf_get_stage_times(self.h, ms))
         return ms
+
+    def set_wait_limit(self, polls: int) -> None:
+        """Poll limit of the bounded device waits (kf_set_wait_limit): 0 makes every
+        bounded wait give up at once, a negative value restores the default."""
+        self._check(self.lib.kf_set_wait_limit(self.h, int(polls)))
 
     def kernels_per_frame(self) -> int:
         n = C.c_int(0)

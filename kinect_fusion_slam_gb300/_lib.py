@@ -123,6 +123,7 @@ SIGNATURES = {
     "kf_enable_stage_timing": (C.c_int, [_H, C.c_int]),
     "kf_get_stage_times": (C.c_int, [_H, _f32p]),
     "kf_kernels_per_frame": (C.c_int, [_H, C.POINTER(C.c_int)]),
+    "kf_set_wait_limit": (C.c_int, [_H, C.c_longlong]),
     "kf_export_ply": (C.c_int, [_H, C.c_char_p, C.c_void_p, C.POINTER(C.c_int)]),
     "kf_save_checkpoint": (C.c_int, [_H, C.c_char_p]),
     "kf_load_checkpoint": (C.c_int, [_H, C.c_char_p]),

@@ -187,7 +187,7 @@ void enq_ingest(kf_handle* h, const uint16_t* raw, bool init_icp, bool normals)
 void enq_bilateral(kf_handle* h)
 {
     launch_bilateral(h->d_depth, h->d_depth_tmp, h->d_spatial, h->cfg.bilateral_radius, h->cfg.sigma_r, h->cam.H,
-                     h->cam.W, h->stream);
+                     h->cam.W, h->d_vmap, h->stream);
     cudaMemcpyAsync(h->d_depth, h->d_depth_tmp, sizeof(float) * h->cam.H * h->cam.W, cudaMemcpyDeviceToDevice,
                     h->stream);
 }
@@ -461,6 +461,7 @@ kf_status reset_state(kf_handle* h)
 {
     KF_TRY(enqueue_clear(h));
     std::memset(h->h_state, 0, sizeof(State));
+    h->h_state->wait_limit = kf::kDefaultWaitLimit;
     for (int k = 0; k < 16; ++k) {
         h->h_state->T[k] = (k % 5 == 0) ? 1.f : 0.f;
         h->h_state->Td[k] = (k % 5 == 0) ? 1.0 : 0.0;
@@ -1273,7 +1274,16 @@ kf_status kf_icp_associate(kf_handle* h, const float F[16], const float T[16], i
     if (pair)
         KF_CUDA(h, cudaMemcpyAsync(pair, h->d_pair, sizeof(int32_t) * h->cam.H * h->cam.W, cudaMemcpyDeviceToHost,
                                    h->stream));
+    int err = 0;
+    KF_CUDA(h, cudaMemcpyAsync(&err, field_ptr<int>(h->d_state, offsetof(State, error)), sizeof(int),
+                               cudaMemcpyDeviceToHost, h->stream));
     KF_CUDA(h, cudaStreamSynchronize(h->stream));
+    if (err) {
+        const int zero = 0;
+        KF_CUDA(h, cudaMemcpy(field_ptr<int>(h->d_state, offsetof(State, error)), &zero, sizeof(int),
+                              cudaMemcpyHostToDevice));
+        return fail(h, KF_ERR_CUDA, "the reduction's bounded wait for a bulk copy gave up; no sums were produced");
+    }
     if (sums27) std::memcpy(sums27, sums, sizeof(float) * 27);
     if (ncorr) *ncorr = (int32_t)sums[kIcpVals - 1];
     return KF_OK;
@@ -1305,6 +1315,18 @@ kf_status kf_get_stage_times(kf_handle* h, float ms[5])
     if (!ms) return fail(h, KF_ERR_INVALID_ARGUMENT, "null output");
     KF_TRY(kf_synchronize(h));
     std::memcpy(ms, h->stage_ms, sizeof(float) * 5);
+    return KF_OK;
+}
+
+kf_status kf_set_wait_limit(kf_handle* h, long long polls)
+{
+    KF_HANDLE(h);
+    const long long v = polls < 0 ? kf::kDefaultWaitLimit : polls;
+    KF_CUDA(h, cudaStreamSynchronize(h->stream));
+    h->h_state->wait_limit = v;
+    KF_CUDA(h, cudaMemcpyAsync(field_ptr<long long>(h->d_state, offsetof(State, wait_limit)), &h->h_state->wait_limit,
+                               sizeof(long long), cudaMemcpyHostToDevice, h->stream));
+    KF_CUDA(h, cudaStreamSynchronize(h->stream));
     return KF_OK;
 }
 

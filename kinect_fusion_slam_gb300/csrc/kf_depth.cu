@@ -125,11 +125,15 @@ constexpr int kBilTx = 32, kBilTy = 8, kBilMaxR = 7;
 // bilateral_filtering.cu:3-47 with the interior bound tightened to y <= H-1-r,
 // x <= W-1-r so the 7x7 window never leaves the image (the reference's `<= H - r`
 // reads one row/column past it); pixels outside the interior are 0, as the reference's
-// zero-initialised output buffer leaves them.
+// zero-initialised output buffer leaves them.  The reference writes the result over
+// depth_image_next, which Estimate_Sensor_Pose then reads as the vertices' z
+// (kinfu_pipeline.cpp:141-160); with vmap given, its z takes the filtered depth too (x, y,
+// the mask and the normals stay those of the unfiltered depth, as in the reference).
 __global__ void __launch_bounds__(kBilTx* kBilTy) bilateral_kernel(const float* __restrict__ depth,
                                                                     float* __restrict__ out,
                                                                     const float* __restrict__ spatial, int r,
-                                                                    float sigma_r, int H, int W)
+                                                                    float sigma_r, int H, int W,
+                                                                    float4* __restrict__ vmap)
 {
     __shared__ float tile[(kBilTy + 2 * kBilMaxR) * (kBilTx + 2 * kBilMaxR)];
     __shared__ float sw[(2 * kBilMaxR + 1) * (2 * kBilMaxR + 1)];
@@ -168,6 +172,7 @@ __global__ void __launch_bounds__(kBilTx* kBilTy) bilateral_kernel(const float* 
         res = acc;
     }
     out[y * W + x] = res;
+    if (vmap) reinterpret_cast<float*>(vmap + y * W + x)[2] = res;
 }
 
 // flip iff acos(c) * (180/pi) > 90 (voxel_traversal.cu:361-364, double acos).  acos is
@@ -202,9 +207,11 @@ __global__ void calibrate_kernel(State* st)
 }
 
 // pose back to identity, ICP bookkeeping and error flag to zero; keeps the calibrated c_flip
+// and the wait limit
 __global__ void state_reset_kernel(State* st)
 {
     const float c_flip = st->c_flip;
+    const long long wait_limit = st->wait_limit;
     __syncthreads();
     unsigned* w = reinterpret_cast<unsigned*>(st);
     for (int i = threadIdx.x; i < (int)(sizeof(State) / sizeof(unsigned)); i += blockDim.x) w[i] = 0u;
@@ -213,7 +220,10 @@ __global__ void state_reset_kernel(State* st)
         st->T[threadIdx.x] = (threadIdx.x % 5 == 0) ? 1.f : 0.f;
         st->Td[threadIdx.x] = (threadIdx.x % 5 == 0) ? 1.0 : 0.0;
     }
-    if (threadIdx.x == 0) st->c_flip = c_flip;
+    if (threadIdx.x == 0) {
+        st->c_flip = c_flip;
+        st->wait_limit = wait_limit;
+    }
 }
 
 // x-fastest (device) <-> z-fastest (reference) volume order
@@ -290,10 +300,10 @@ void launch_vertex(const uint16_t* raw, float* depth, float4* vmap, float4* nmap
 const void* vertex_raw_kernel_func() { return reinterpret_cast<const void*>(&vertex_kernel<true>); }
 
 void launch_bilateral(const float* depth, float* out, const float* spatial, int r, float sigma_r, int H, int W,
-                      cudaStream_t s)
+                      float4* vmap, cudaStream_t s)
 {
     dim3 block(kBilTx, kBilTy), grid((W + kBilTx - 1) / kBilTx, (H + kBilTy - 1) / kBilTy);
-    bilateral_kernel<<<grid, block, 0, s>>>(depth, out, spatial, r, sigma_r, H, W);
+    bilateral_kernel<<<grid, block, 0, s>>>(depth, out, spatial, r, sigma_r, H, W, vmap);
 }
 
 void launch_calibrate(State* st, cudaStream_t s) { calibrate_kernel<<<1, 32, 0, s>>>(st); }

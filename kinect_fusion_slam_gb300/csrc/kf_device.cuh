@@ -60,7 +60,13 @@ struct State {
     float Tlog[kMaxIcpIters][16];  // pose after each iteration
     float sums[kIcpVals];  // sums of the most recent ICP iteration
     unsigned fix_bad;      // precision form: sums whose block values could not be accumulated
+    // polls a bounded wait makes before it gives up and sets error (kept across resets;
+    // kDefaultWaitLimit unless a test lowers it to exercise the error path)
+    long long wait_limit;
 };
+
+// about 1 s of polling: a copy or a peer that has not arrived by then is reported
+constexpr long long kDefaultWaitLimit = 1LL << 26;
 
 // One scene of a batch (the batching form): the device buffers and parameters its
 // kernels need.  A batched launch covers every scene; blockIdx.y (or a flattened tile

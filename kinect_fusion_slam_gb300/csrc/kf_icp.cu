@@ -620,8 +620,6 @@ constexpr int kBatch = 16;
 constexpr int kBatchesPerChunk = kChunkGroups / kBatch;
 static_assert(kChunkGroups % (2 * kBatch) == 0, "a chunk is an even number of batches");
 constexpr unsigned kChunkBytes = kChunkGroups * kIcpVals * 4u;  // multiple of 16
-// bounded waits: a copy that has not landed after this many polls is reported, not awaited
-constexpr long long kMaxPolls = 1LL << 26;
 
 __device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
 
@@ -635,9 +633,12 @@ __device__ __forceinline__ void bulk_load(void* dst, const void* src, unsigned b
                  : "memory");
 }
 
-__device__ __forceinline__ bool bar_wait(unsigned long long* bar, unsigned parity)
+// bounded wait for the phase of the given parity: false once `limit` polls have passed
+// without it (State::wait_limit; a copy that has not landed by then is reported, not
+// awaited)
+__device__ __forceinline__ bool bar_wait(unsigned long long* bar, unsigned parity, long long limit)
 {
-    for (long long i = 0; i < kMaxPolls; ++i) {
+    for (long long i = 0; i < limit; ++i) {
         unsigned done;
         asm volatile(
             "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
@@ -659,6 +660,7 @@ __device__ __forceinline__ void solve_body(const float* __restrict__ partials, i
     __shared__ float red[kIcpVals];
     __shared__ float sT0[16], sTp[16];
     const int lane = threadIdx.x;
+    const long long limit = st->wait_limit;
     // the pose inputs of the solve, loaded now so their latency hides behind the sums
     float t0 = 0.f, tp = 0.f;
     int it = 0;
@@ -680,11 +682,13 @@ __device__ __forceinline__ void solve_body(const float* __restrict__ partials, i
                       chunk_bytes(c), &bars[c]);
     }
     __syncwarp();
+    // chunks issued so far (uniform over the warp), and the chunk whose wait gave up
+    int issued = min(kBuffers, nchunks), failed_at = 0;
     // lanes 28..31 read term 27's column too (in bounds) and discard it
     const int term = lane < kIcpVals ? lane : kIcpVals - 1;
     auto slot_ptr = [&](int c) { return buf + (c % kBuffers) * kChunkGroups * kIcpVals + term; };
     float sum = 0.f;
-    bool ok = nchunks == 0 || bar_wait(&bars[0], 0);
+    bool ok = nchunks == 0 || bar_wait(&bars[0], 0, limit);
     const int full = ngroups / kChunkGroups;  // chunks of exactly kChunkGroups groups
     float va[kBatch], vb[kBatch];
     if (ok && full > 0) {
@@ -717,7 +721,8 @@ __device__ __forceinline__ void solve_body(const float* __restrict__ partials, i
         }
         // open the next full chunk before the last batch's additions
         if (c + 1 < full) {
-            ok = bar_wait(&bars[(c + 1) % kBuffers], ((c + 1) / kBuffers) & 1);
+            ok = bar_wait(&bars[(c + 1) % kBuffers], ((c + 1) / kBuffers) & 1, limit);
+            if (!ok) failed_at = c + 1;
             const float* pn = slot_ptr(c + 1);
 #pragma unroll
             for (int q = 0; q < kBatch; ++q) va[q] = ok ? pn[q * kIcpVals] : 0.f;
@@ -726,17 +731,23 @@ __device__ __forceinline__ void solve_body(const float* __restrict__ partials, i
         for (int q = 0; q < kBatch; ++q) sum = sum + vb[q];
         // every group of chunk c is added: its slot goes back to the copy engine
         __syncwarp();
-        if (lane == 0 && c + kBuffers < nchunks) {
-            // the warp's reads of this slot precede the async-proxy write that refills it
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            bulk_load(buf + (c % kBuffers) * kChunkGroups * kIcpVals,
-                      partials + (size_t)(c + kBuffers) * kChunkGroups * kIcpVals, chunk_bytes(c + kBuffers),
-                      &bars[c % kBuffers]);
+        if (ok && c + kBuffers < nchunks) {
+            if (lane == 0) {
+                // the warp's reads of this slot precede the async-proxy write that refills it
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                bulk_load(buf + (c % kBuffers) * kChunkGroups * kIcpVals,
+                          partials + (size_t)(c + kBuffers) * kChunkGroups * kIcpVals, chunk_bytes(c + kBuffers),
+                          &bars[c % kBuffers]);
+            }
+            issued = c + kBuffers + 1;
         }
     }
     if (ok && full < nchunks) {
         // the last, partial chunk, in batches without prefetch
-        if (full > 0) ok = bar_wait(&bars[full % kBuffers], (full / kBuffers) & 1);
+        if (full > 0) {
+            ok = bar_wait(&bars[full % kBuffers], (full / kBuffers) & 1, limit);
+            if (!ok) failed_at = full;
+        }
         if (ok) {
             const float* p = slot_ptr(full);
             const int cnt = ngroups - full * kChunkGroups;
@@ -751,12 +762,16 @@ __device__ __forceinline__ void solve_body(const float* __restrict__ partials, i
         }
     }
     if (!ok) {
-        // a bulk copy did not complete: report it, give the copies in flight a bounded
-        // wait, and leave the pose as it is
-        if (lane == 0) {
-            st->error = 1;
-            for (int k = 0; k < kBuffers; ++k) bar_wait(&bars[k], 0);
-        }
+        // A bulk copy did not complete within the limit: report it, and leave the pose as
+        // it is (MODE 1 writes NaN sums, so a failed reduction cannot pass for a result).
+        // The copies still in flight -- chunks failed_at .. issued-1, each the only one
+        // outstanding on its buffer -- get a bounded wait at the default limit before the
+        // block exits, so none lands in shared memory the block no longer owns.
+        if (lane == 0) st->error = 1;
+        if (MODE == 1 && lane < kIcpVals) sums_out[lane] = qnan();
+        if (lane == 0)
+            for (int c = failed_at; c < issued; ++c)
+                bar_wait(&bars[c % kBuffers], (c / kBuffers) & 1, kDefaultWaitLimit);
         return;
     }
     if (lane < kIcpVals) red[lane] = sum;

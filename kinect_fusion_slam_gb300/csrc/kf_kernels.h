@@ -23,9 +23,10 @@ const void* vertex_raw_kernel_func();
 void launch_vertex(const uint16_t* raw, float* depth, float4* vmap, float4* nmap, const Camera& cam, float dmin,
                    float dmax, State* st, bool init_icp, bool compute_normals, cudaStream_t s);
 
-// 7x7 (radius r) bilateral filter of depth into out (bilateral_filtering.cu:3-47)
+// 7x7 (radius r) bilateral filter of depth into out (bilateral_filtering.cu:3-47); vmap
+// (may be nullptr): the vertex map whose z takes the filtered depth
 void launch_bilateral(const float* depth, float* out, const float* spatial, int r, float sigma_r, int H, int W,
-                      cudaStream_t s);
+                      float4* vmap, cudaStream_t s);
 
 // One ICP iteration: association + one-pass reduction + (last block) 6x6 solve and pose
 // update.  partials must hold icp_grid_blocks() * kIcpVals floats.

@@ -13,6 +13,8 @@
 //            returns false and leaves b untouched when a pivot is below FLT_EPSILON.
 // Every file that includes this is compiled without FMA contraction (-fmad=false on
 // the device, -ffp-contract=off on the host), so host and device give the same bits.
+// Attribution: these algorithms are OpenCV's (https://opencv.org, Apache License 2.0),
+// restated here; no OpenCV source is included.
 #pragma once
 
 #include <cfloat>

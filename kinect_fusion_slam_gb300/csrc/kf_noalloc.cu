@@ -44,7 +44,8 @@ struct Mats {
     float T[16];
 };
 
-// writes the call's transforms into the scratch and zeroes the completion counter
+// writes the call's transforms into the scratch and zeroes the completion counter and
+// the error flag (the reduction's bounded waits run at their default limit)
 __global__ void noalloc_prepare_kernel(Mats m)
 {
     float* mats = reinterpret_cast<float*>(g_noalloc_scratch + kMatsOff);
@@ -52,7 +53,12 @@ __global__ void noalloc_prepare_kernel(Mats m)
         mats[threadIdx.x] = m.F[threadIdx.x];
         mats[16 + threadIdx.x] = m.T[threadIdx.x];
     }
-    if (threadIdx.x == 0) reinterpret_cast<kf::State*>(g_noalloc_scratch + kStateOff)->ticket = 0u;
+    if (threadIdx.x == 0) {
+        kf::State* st = reinterpret_cast<kf::State*>(g_noalloc_scratch + kStateOff);
+        st->ticket = 0u;
+        st->error = 0;
+        st->wait_limit = kf::kDefaultWaitLimit;
+    }
 }
 
 std::mutex g_mu;
@@ -92,6 +98,13 @@ extern "C" kf_status kf_icp_associate_noalloc(int height, int width, const float
     if (!aligned16(vmap) || !aligned16(nmap) || !aligned16(pred_v) || !aligned16(pred_n))
         return KF_ERR_INVALID_ARGUMENT;
     if (!(dist_mm >= 0.f) || !(angle_deg >= 0.f)) return KF_ERR_INVALID_ARGUMENT;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (s) {
+        // the scratch address below is the current device's: the stream must be on it
+        int cur = 0, sdev = 0;
+        if (cudaGetDevice(&cur) != cudaSuccess || cudaStreamGetDevice(s, &sdev) != cudaSuccess) return KF_ERR_CUDA;
+        if (sdev != cur) return KF_ERR_INVALID_ARGUMENT;
+    }
     unsigned char* base = nullptr;
     if (scratch_base(&base) != cudaSuccess) return KF_ERR_CUDA;
 
@@ -107,7 +120,6 @@ extern "C" kf_status kf_icp_associate_noalloc(int height, int width, const float
         m.F[k] = F[k];
         m.T[k] = T[k];
     }
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
     noalloc_prepare_kernel<<<1, 32, 0, s>>>(m);
     const float* mats = reinterpret_cast<const float*>(base + kMatsOff);
     kf::launch_icp_associate(reinterpret_cast<const float4*>(vmap), reinterpret_cast<const float4*>(nmap),

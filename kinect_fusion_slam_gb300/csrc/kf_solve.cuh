@@ -17,6 +17,8 @@
 // (about one entry in 10^4 on random systems, more under heavy cancellation) the entry
 // is recomputed by the FP64 sequence itself.  Every file that includes this is
 // compiled with -fmad=false, so the float expressions below are evaluated as written.
+// Attribution: cv::Cholesky's and cv::gemm's algorithms are OpenCV's (https://opencv.org,
+// Apache License 2.0), restated here; no OpenCV source is included.
 #pragma once
 
 #include <cfloat>

@@ -7,7 +7,7 @@ contract a*b+c into an FMA):
 * ``oracle/libkf_oracle.so`` -- the restatement in ``kf_oracle.cpp`` and the FP64
   oracle in ``kf_oracle64.cpp``.
 * ``oracle/_ref/libkf_ref.so`` -- the reference's own kernel bodies.  When the
-  reference tree is available (``KF_REF_DIR``, default ``/root/reference``) this
+  reference tree is available (its location in ``KF_REF_DIR``; no default) this
   splices the kernel bodies out of its ``src/parallel_processing`` sources into
   ``oracle/_ref/ref_kernels.inc`` (never committed: ``oracle/_ref/`` is git-ignored)
   and compiles them with ``ref_harness.cpp``.  Where the tree is absent but an
@@ -59,8 +59,10 @@ _SUBST = {
 }
 
 
-def reference_dir() -> Path:
-    return Path(os.environ.get("KF_REF_DIR", "/root/reference"))
+def reference_dir() -> Path | None:
+    """The reference checkout named by KF_REF_DIR, or None (no splice is made)."""
+    ref = os.environ.get("KF_REF_DIR")
+    return Path(ref) if ref else None
 
 
 def _newer(target: Path, sources) -> bool:
@@ -73,6 +75,8 @@ def _newer(target: Path, sources) -> bool:
 def splice_reference(ref_dir: Path | None = None) -> Path | None:
     """Write oracle/_ref/ref_kernels.inc from the reference sources; None if absent."""
     ref_dir = ref_dir or reference_dir()
+    if ref_dir is None:
+        return None
     src_dir = ref_dir / "src" / "parallel_processing"
     if not src_dir.is_dir():
         return None

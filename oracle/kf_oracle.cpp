@@ -595,6 +595,9 @@ struct kfo_pipeline {
     int icp_iters;
     int levels = 1, level_iters[3] = {10, 0, 0};
     float band = 90.f;
+    int bilateral = 0, bil_r = 3;
+    float sigma_r = 30.f;
+    std::vector<float> spatial, filtered;
     std::vector<float> tsdf, weight, depth, cur6, pred6;
     std::vector<uint8_t> mask;
     std::vector<int32_t> hit;
@@ -644,13 +647,49 @@ void kfo_set_pyramid(kfo_pipeline* p, int levels, const int* iters, float band)
     p->band = band;
 }
 
-void kfo_incoming(kfo_pipeline* p, const uint16_t* raw)
+/* the bilateral stage at the reference's commented-out call site
+ * (kinfu_pipeline.cpp:141-145): its spatial kernel as SystemUtility::CreateSpatialKernel
+ * (system_utility.cpp:94-113) */
+void kfo_set_bilateral(kfo_pipeline* p, int enable, int radius, float sigma_d, float sigma_r)
+{
+    p->bilateral = enable != 0;
+    p->bil_r = radius;
+    p->sigma_r = sigma_r;
+    const int kl = 2 * radius + 1;
+    p->spatial.assign((size_t)kl * kl, 0.f);
+    for (int y = -radius; y <= radius; ++y)
+        for (int x = -radius; x <= radius; ++x) {
+            const float e = -((float)(x * x) + (float)(y * y)) / (2 * sigma_d * sigma_d);
+            p->spatial[(y + radius) * kl + (x + radius)] = (float)std::exp((double)e);
+        }
+}
+
+static void incoming(kfo_pipeline* p, const uint16_t* raw, const float* filtered_in);
+
+void kfo_incoming(kfo_pipeline* p, const uint16_t* raw) { incoming(p, raw, nullptr); }
+
+void kfo_incoming_filtered(kfo_pipeline* p, const uint16_t* raw, const float* filtered)
+{
+    incoming(p, raw, filtered);
+}
+
+static void incoming(kfo_pipeline* p, const uint16_t* raw, const float* filtered_in)
 {
     const int H = p->H, W = p->W;
     const long HW = (long)H * W;
     kfo_depth_ingest(raw, H * W, p->min_depth, p->max_depth, p->depth.data());
     float* c = p->cur6.data();
     kfo_vertex_normal(H, W, p->depth.data(), p->Ki, c, c + HW, c + 3 * HW, c + 4 * HW, c + 5 * HW, p->mask.data());
+    if (p->bilateral) {
+        /* Bilateral_Filtering writes over depth_image_next, which ICP then reads as the
+         * vertices' z and integration and the ray cast as the depth */
+        p->filtered.assign(HW, 0.f);
+        if (filtered_in)
+            std::memcpy(p->filtered.data(), filtered_in, sizeof(float) * HW);
+        else
+            kfo_bilateral(H, W, p->depth.data(), p->spatial.data(), p->bil_r, p->sigma_r, p->filtered.data());
+        p->depth = p->filtered;
+    }
     std::memcpy(c + 2 * HW, p->depth.data(), sizeof(float) * HW);
     if (p->levels == 1) {
         kfo_estimate_pose(H, W, p->K, p->T, c, p->mask.data(), p->pred6.data(), p->icp_iters, nullptr, nullptr,

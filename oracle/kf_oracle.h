@@ -88,8 +88,13 @@ kfo_pipeline* kfo_create(int H, int W, float min_depth, float max_depth, const k
 void kfo_destroy(kfo_pipeline* p);
 /* InitialProcessing (kinfu_pipeline.cpp:91-119) */
 void kfo_initial(kfo_pipeline* p, const uint16_t* raw);
-/* IncomingFrameProcessing (kinfu_pipeline.cpp:121-193), bilateral disabled as in the reference */
+/* IncomingFrameProcessing (kinfu_pipeline.cpp:121-193), bilateral disabled as in the
+ * reference unless kfo_set_bilateral enabled it */
 void kfo_incoming(kfo_pipeline* p, const uint16_t* raw);
+/* the bilateral stage at the reference's commented-out call site (kinfu_pipeline.cpp:141-145) */
+void kfo_set_bilateral(kfo_pipeline* p, int enable, int radius, float sigma_d, float sigma_r);
+/* kfo_incoming with the bilateral stage's output given (H*W floats) instead of computed */
+void kfo_incoming_filtered(kfo_pipeline* p, const uint16_t* raw, const float* filtered);
 /* ICP pyramid (not in the reference): levels 1..3, iterations per level finest first,
  * depth-similarity band of the block averaging (mm) */
 void kfo_set_pyramid(kfo_pipeline* p, int levels, const int* iters, float band);

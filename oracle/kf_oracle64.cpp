@@ -10,7 +10,7 @@
  * zero-crossing interpolation and the never-assigned axis records pinned to 0, the
  * uncapped weight -- so the only difference from the reference is precision.  The
  * precision form of the GPU pipeline (FP16 TSDF, compensated FP32 sums, FP64 solve) is
- * judged by its TSDF, prediction and trajectory error against this run.
+ * measured by its TSDF, prediction and trajectory error against this run.
  */
 #include "kf_oracle.h"
 

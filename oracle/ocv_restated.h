@@ -22,6 +22,9 @@
  *                 forward/back substitution.  Returns 0 (and leaves b untouched) when
  *                 a pivot falls below FLT_EPSILON.  sensor_pose_estimation.cu:399.
  *
+ * Attribution: the algorithms restated here are OpenCV's (https://opencv.org,
+ * Apache License 2.0); no OpenCV source is included.
+ *
  * Parity for these four pieces is unpinned: no OpenCV build exists here to test
  * against.  The product restates the same algorithms independently in
  * kinect_fusion_slam_gb300/csrc/kf_math.cuh, and the tests check the two agree

@@ -143,6 +143,8 @@ class Oracle(_Common):
         self._fn("kfo_destroy", None, [C.c_void_p])
         self._fn("kfo_initial", None, [C.c_void_p, _u16p])
         self._fn("kfo_incoming", None, [C.c_void_p, _u16p])
+        self._fn("kfo_set_bilateral", None, [C.c_void_p, C.c_int, C.c_int, C.c_float, C.c_float])
+        self._fn("kfo_incoming_filtered", None, [C.c_void_p, _u16p, _f32p])
         self._fn("kfo_get_pose", None, [C.c_void_p, _f32p])
         self._fn("kfo_set_pose", None, [C.c_void_p, _f32p])
         self._fn("kfo_get_prediction", None, [C.c_void_p, C.c_void_p, C.c_void_p])
@@ -303,8 +305,18 @@ class OraclePipeline:
     def initial(self, raw):
         self.o.lib.kfo_initial(self.h, np.ascontiguousarray(raw, np.uint16).ravel())
 
-    def incoming(self, raw):
-        self.o.lib.kfo_incoming(self.h, np.ascontiguousarray(raw, np.uint16).ravel())
+    def incoming(self, raw, filtered=None):
+        """IncomingFrameProcessing; with the bilateral stage on, `filtered` (H x W float)
+        replaces the stage's own output."""
+        raw = np.ascontiguousarray(raw, np.uint16).ravel()
+        if filtered is None:
+            self.o.lib.kfo_incoming(self.h, raw)
+        else:
+            self.o.lib.kfo_incoming_filtered(self.h, raw, _c32(filtered).ravel())
+
+    def set_bilateral(self, enable=True, radius=3, sigma_d=4.5, sigma_r=30.0):
+        """The bilateral stage at the reference's commented-out call site."""
+        self.o.lib.kfo_set_bilateral(self.h, int(enable), int(radius), float(sigma_d), float(sigma_r))
 
     def set_pyramid(self, levels, iterations, band=90.0):
         """ICP pyramid: iterations per level, finest first."""

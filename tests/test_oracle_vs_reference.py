@@ -5,7 +5,7 @@ ICP sums, and the poses of whole frame sequences."""
 import numpy as np
 import pytest
 
-from conftest import REF_DATA, grid_spec, real_frame
+from conftest import grid_spec, real_frame
 
 
 def bits(a):
@@ -94,7 +94,6 @@ def test_pipeline_synthetic(oracle, reference, small_seq):
 
 
 @pytest.mark.slow
-@pytest.mark.skipif(not (REF_DATA / "dep0025.dat").exists(), reason="reference data not present")
 def test_pipeline_real_frames(oracle, reference):
     """The reference's default configuration on its own recorded frames 25..27."""
     from oracle.pyoracle import GridSpec, reference_K
