@@ -267,6 +267,14 @@ kf_status kf_render_trilinear_backward(const kf_render_desc* d, const float* tsd
 kf_status kf_render_depth_normal_equations(const kf_render_desc* d, const float* tsdf, const float T[16],
                                            const float* measured_depth, float max_residual, double sums[29],
                                            void* stream);
+/* The same under a Huber loss with threshold huber_delta (mm; 0 gives the call above):
+ * each pixel's terms are weighted by min(1, huber_delta / |r|) (iteratively reweighted
+ * Gauss-Newton), so sums[21..26] = J^T psi(r) with psi(r) = clamp(r, -delta, delta), the
+ * loss's gradient; sums[28] = sum of 2 rho(r) (r^2 inside the threshold, 2 delta |r| -
+ * delta^2 outside).  Synchronous. */
+kf_status kf_render_depth_normal_equations_huber(const kf_render_desc* d, const float* tsdf, const float T[16],
+                                                 const float* measured_depth, float max_residual, float huber_delta,
+                                                 double sums[29], void* stream);
 
 /* ---- batching form: many scenes, one launch per stage, one graph per frame --------
  * No counterpart in the reference.  A batch owns one kf_handle per scene; the scenes
@@ -295,6 +303,12 @@ kf_status kf_batch_kernels_per_frame(kf_batch* b, int* n);
  * (8, 16, 32; not timed: integration updates the volume).  Synchronous. */
 kf_status kf_batch_autotune(kf_batch* b, int tuning[4]);
 kf_status kf_batch_set_tuning(kf_batch* b, const int tuning[4]);
+/* How integration and the ICP group pass spread the scenes' work: 0 (default) a 2-D
+ * grid, one row of blocks per scene (blocks past a smaller scene's extent return at
+ * once); 1 a fixed grid over the flattened work of all scenes -- integration boxes taken
+ * one at a time from one counter, ICP groups in static strides -- as the ray cast always
+ * does.  Results are identical either way.  Synchronous. */
+kf_status kf_batch_set_forms(kf_batch* b, int persistent_integration, int persistent_icp);
 
 /* ---- timing --------------------------------------------------------------------- */
 /* per-stage device time of the latest kf_incoming_frame (CUDA events, ms):

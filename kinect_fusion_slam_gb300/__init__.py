@@ -416,3 +416,8 @@ class Batch:
     def set_tuning(self, tuning) -> None:
         self._check(self.lib.kf_batch_set_tuning(self.b, (C.c_int * 4)(*tuning)))
 
+    def set_forms(self, persistent_integration: bool, persistent_icp: bool) -> None:
+        """kf_batch_set_forms: spread integration / the ICP group pass over a fixed grid
+        covering every scene's work (True) or one row of blocks per scene (False)."""
+        self._check(self.lib.kf_batch_set_forms(self.b, int(persistent_integration), int(persistent_icp)))
+

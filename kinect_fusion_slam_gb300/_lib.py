@@ -132,6 +132,8 @@ SIGNATURES = {
                                                C.c_void_p, C.c_void_p, C.c_void_p]),
     "kf_render_depth_normal_equations": (C.c_int, [C.POINTER(RenderDesc), C.c_void_p, _f32p, C.c_void_p, C.c_float,
                                                    C.POINTER(C.c_double), C.c_void_p]),
+    "kf_render_depth_normal_equations_huber": (C.c_int, [C.POINTER(RenderDesc), C.c_void_p, _f32p, C.c_void_p,
+                                                         C.c_float, C.c_float, C.POINTER(C.c_double), C.c_void_p]),
     "kf_batch_create": (C.c_int, [C.POINTER(Config), C.c_int, C.POINTER(C.c_void_p)]),
     "kf_batch_destroy": (C.c_int, [C.c_void_p]),
     "kf_batch_scene": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(_H)]),
@@ -141,6 +143,7 @@ SIGNATURES = {
     "kf_batch_kernels_per_frame": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
     "kf_batch_autotune": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
     "kf_batch_set_tuning": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
+    "kf_batch_set_forms": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "kf_selftest_solve": (C.c_int, [C.c_ulonglong, C.c_int, C.c_int, C.POINTER(C.c_ulonglong)]),
     "kf_selftest_solve6": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
     "kf_icp_associate_noalloc": (C.c_int, [C.c_int, C.c_int, _f32p, _f32p, _f32p, _vp, _vp, _vp, _vp, C.c_float,

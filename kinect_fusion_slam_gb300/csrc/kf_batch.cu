@@ -31,6 +31,11 @@ struct kf_batch {
     int max_pixels[kMaxLevels] = {}, max_groups[kMaxLevels] = {};
     int tuning[4] = {8, 0, 4, 16};  // group warps, ray shape, ray blocks per SM, z chunk
     int sms = 152;
+    // which stages run over the flattened work of all scenes on a fixed grid (1) rather
+    // than as a 2-D grid with a row of blocks per scene (0): integration, ICP group pass
+    int persist_int = 0, persist_icp = 0;
+    unsigned* d_work = nullptr;  // integration's box counter pair
+    unsigned total_boxes = 0, total_groups[kMaxLevels] = {};
     cudaGraphExec_t g_initial = nullptr, g_incoming = nullptr;
 };
 
@@ -47,6 +52,7 @@ void destroy_graphs(kf_batch* b)
 void fill_table(kf_batch* b)
 {
     int start[3] = {0, 0, 0};
+    unsigned boxes = 0, groups[kMaxLevels] = {};
     for (int i = 0; i < b->n; ++i) {
         const kf_handle* h = b->scenes[i];
         SceneDev& d = b->h_table[i];
@@ -81,7 +87,15 @@ void fill_table(kf_batch* b)
             d.tile_start[sh] = start[sh];
             start[sh] += raycast_tiles(h->cam.H, h->cam.W, sh);
         }
+        d.int_start = (int)boxes;
+        boxes += (unsigned)integrate_tiles(h->grid, b->tuning[3]);
+        for (int l = 0; l < kMaxLevels; ++l) {
+            d.grp_start[l] = (int)groups[l];
+            groups[l] += (unsigned)((h->lcam[l].H * h->lcam[l].W + 63) / 64);
+        }
     }
+    b->total_boxes = boxes;
+    for (int l = 0; l < kMaxLevels; ++l) b->total_groups[l] = groups[l];
 }
 
 unsigned total_ray_tiles(const kf_batch* b, int shape)
@@ -108,11 +122,21 @@ void enq_frame(kf_batch* b, bool incoming)
             launch_vertex_batch(b->d_table, b->n, b->max_pixels[l], l, false, s);
         }
         for (int l = b->levels - 1; l >= 0; --l)
-            for (int it = 0; it < b->iters[l]; ++it)
-                launch_icp_iteration_batch(b->d_table, b->n, b->max_groups[l], l, b->tuning[0], s);
+            for (int it = 0; it < b->iters[l]; ++it) {
+                if (b->persist_icp)
+                    launch_icp_iteration_batch_persistent(b->d_table, b->n, b->max_groups[l], l, b->total_groups[l],
+                                                          4 * b->sms, s);
+                else
+                    launch_icp_iteration_batch(b->d_table, b->n, b->max_groups[l], l, b->tuning[0], s);
+            }
     }
     const int zc = b->tuning[3];
-    launch_integrate_batch(b->d_table, b->n, b->max_pixels[0], max_integrate_tiles(b, zc), zc, b->f16, !incoming, s);
+    if (b->persist_int)
+        launch_integrate_batch_persistent(b->d_table, b->n, b->max_pixels[0], b->total_boxes, zc, b->f16, !incoming,
+                                          5 * b->sms, b->d_work, s);
+    else
+        launch_integrate_batch(b->d_table, b->n, b->max_pixels[0], max_integrate_tiles(b, zc), zc, b->f16, !incoming,
+                               s);
     launch_raycast_batch(b->d_table, b->n, total_ray_tiles(b, b->tuning[1]), b->f16, b->tuning[1],
                          b->tuning[2] * b->sms, b->d_tiles, s);
 }
@@ -184,7 +208,9 @@ kf_status kf_batch_create(const kf_config* configs, int n_scenes, kf_batch** out
     if (s == KF_OK && (cudaMallocHost((void**)&b->h_table, sizeof(SceneDev) * n_scenes) != cudaSuccess ||
                        cudaMalloc((void**)&b->d_table, sizeof(SceneDev) * n_scenes) != cudaSuccess ||
                        cudaMalloc((void**)&b->d_tiles, 2 * sizeof(unsigned)) != cudaSuccess ||
-                       cudaMemset(b->d_tiles, 0, 2 * sizeof(unsigned)) != cudaSuccess))
+                       cudaMemset(b->d_tiles, 0, 2 * sizeof(unsigned)) != cudaSuccess ||
+                       cudaMalloc((void**)&b->d_work, 2 * sizeof(unsigned)) != cudaSuccess ||
+                       cudaMemset(b->d_work, 0, 2 * sizeof(unsigned)) != cudaSuccess))
         s = KF_ERR_OUT_OF_MEMORY;
     if (s == KF_OK) {
         std::memset(b->h_table, 0, sizeof(SceneDev) * n_scenes);
@@ -217,6 +243,7 @@ kf_status kf_batch_destroy(kf_batch* b)
     if (b->h_table) cudaFreeHost(b->h_table);
     if (b->d_table) cudaFree(b->d_table);
     if (b->d_tiles) cudaFree(b->d_tiles);
+    if (b->d_work) cudaFree(b->d_work);
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
     return KF_OK;
@@ -269,6 +296,19 @@ kf_status kf_batch_set_tuning(kf_batch* b, const int tuning[4])
     if (!ok) return KF_ERR_INVALID_ARGUMENT;
     if (cudaStreamSynchronize(b->stream) != cudaSuccess) return KF_ERR_CUDA;
     std::memcpy(b->tuning, tuning, sizeof(b->tuning));
+    fill_table(b);  // the flattened box list depends on the z chunk
+    if (cudaMemcpy(b->d_table, b->h_table, sizeof(SceneDev) * b->n, cudaMemcpyHostToDevice) != cudaSuccess)
+        return KF_ERR_CUDA;
+    destroy_graphs(b);
+    return KF_OK;
+}
+
+kf_status kf_batch_set_forms(kf_batch* b, int persistent_integration, int persistent_icp)
+{
+    if (!b) return KF_ERR_INVALID_ARGUMENT;
+    if (cudaStreamSynchronize(b->stream) != cudaSuccess) return KF_ERR_CUDA;
+    b->persist_int = persistent_integration != 0;
+    b->persist_icp = persistent_icp != 0;
     destroy_graphs(b);
     return KF_OK;
 }

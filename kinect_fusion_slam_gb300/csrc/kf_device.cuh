@@ -96,6 +96,10 @@ struct SceneDev {
     int tile_start[3];  // first ray-cast tile of this scene for tile shapes 8x4, 16x2, 4x8
     float depth_eps;    // integration's depth-band cull margin (depth_band_eps)
     float lam_max;      // ray_norm_max
+    // the scene's first integration box and first ICP group (per pyramid level) in the
+    // batch's flattened lists, for the launches that spread all scenes' work over the GPU
+    int int_start;
+    int grp_start[kMaxBatchLevels];
 };
 
 // voxel-centre coordinate, kinfu_pipeline.cpp:53-55: x * voxel_distance + voxel_distance / 2

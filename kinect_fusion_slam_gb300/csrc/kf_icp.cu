@@ -605,6 +605,36 @@ __global__ void __launch_bounds__(WARPS * 32) icp_group_batch_kernel(const Scene
                       d.partials, d.groups, nullptr);
 }
 
+// the group pass of every scene of a batch at `level`, spread over a fixed grid: warp w
+// of the grid takes the groups w, w + W, w + 2W, ... of the flattened list of all scenes'
+// groups (scene s owns groups [grp_start of s, grp_start of s + 1)); groups cost about
+// the same, so a static share needs no counter
+template <int WARPS>
+__global__ void __launch_bounds__(WARPS * 32) icp_group_batch_persist_kernel(const SceneDev* __restrict__ scenes,
+                                                                           int n_scenes, int level, unsigned total)
+{
+    wait_for_producer();
+    __shared__ float sF[WARPS][16], sT[WARPS][16];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int cur = -1;
+    for (unsigned g = blockIdx.x * WARPS + warp; g < total; g += gridDim.x * WARPS) {
+        int s = 0;
+        while (s + 1 < n_scenes && g >= (unsigned)scenes[s + 1].grp_start[level]) ++s;
+        const SceneDev& d = scenes[s];
+        if (s != cur) {
+            __syncwarp();
+            if (lane < 16) {
+                sF[warp][lane] = d.st->F[lane];
+                sT[warp][lane] = d.st->T[lane];
+            }
+            __syncwarp();
+            cur = s;
+        }
+        group_sums<0>((int)(g - (unsigned)d.grp_start[level]), lane, d.vmap[level], d.nmap[level], d.pv[level],
+                      d.pn[level], d.cam[level], d.icp, sF[warp], sT[warp], d.partials, d.groups, nullptr);
+    }
+}
+
 // Reduce-and-solve pass: one warp.  The group sums are streamed into shared memory in
 // order by the bulk-copy engine (cp.async.bulk into a ring of kBuffers chunks with
 // mbarrier completion; kBuffers - 1 copies stay in flight) while the warp adds them:
@@ -1190,6 +1220,15 @@ void launch_icp_iteration_batch(const SceneDev* scenes, int n_scenes, int max_gr
     default:
         launch_pdl(icp_group_batch_kernel<8>, dim3((max_groups + 7) / 8, n_scenes), dim3(8 * 32), 0, s, scenes, level);
     }
+    launch_pdl(icp_solve_batch_kernel, dim3(n_scenes), dim3(32), solve_smem_bytes(max_groups), s, scenes, level);
+}
+
+void launch_icp_iteration_batch_persistent(const SceneDev* scenes, int n_scenes, int max_groups, int level,
+                                           unsigned total_groups, int blocks, cudaStream_t s)
+{
+    ensure_solve_smem(max_groups);
+    launch_pdl(icp_group_batch_persist_kernel<8>, dim3(blocks), dim3(8 * 32), 0, s, scenes, n_scenes, level,
+               total_groups);
     launch_pdl(icp_solve_batch_kernel, dim3(n_scenes), dim3(32), solve_smem_bytes(max_groups), s, scenes, level);
 }
 

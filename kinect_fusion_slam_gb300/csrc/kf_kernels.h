@@ -110,6 +110,14 @@ int integrate_tiles(const Grid& g, int zchunk);
 int raycast_tiles(int H, int W, int shape);
 void launch_raycast_batch(const SceneDev* scenes, int n_scenes, unsigned total_tiles, bool f16, int shape,
                           int blocks, unsigned* tile_counter, cudaStream_t s);
+// the same with the group pass spread over a fixed grid of `blocks` 8-warp blocks (warps
+// stride over the flattened groups of all scenes; SceneDev::grp_start must be filled)
+void launch_icp_iteration_batch_persistent(const SceneDev* scenes, int n_scenes, int max_groups, int level,
+                                           unsigned total_groups, int blocks, cudaStream_t s);
+// integration prep + a persistent integration over all scenes' boxes from one counter
+// (two device unsigneds, zero between launches; SceneDev::int_start for this zchunk)
+void launch_integrate_batch_persistent(const SceneDev* scenes, int n_scenes, int max_pixels, unsigned total_boxes,
+                                       int zchunk, bool f16, bool first, int blocks, unsigned* counter, cudaStream_t s);
 // the group pass alone (idempotent: what the autotuner times)
 void launch_icp_group_batch(const SceneDev* scenes, int n_scenes, int max_groups, int level, int warps, cudaStream_t s);
 // packs the predicted points with z != 0 into out (2 float4 per point, unordered) and

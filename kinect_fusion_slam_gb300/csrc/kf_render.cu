@@ -41,6 +41,7 @@ struct RenderGeom {
     float t_near, t_far, step;
     int max_steps;
     float max_residual;  // Gauss-Newton gate (infinity = none)
+    float huber;         // Huber threshold of the normal equations (0 = plain least squares)
 };
 
 struct Corner8 {
@@ -303,15 +304,21 @@ __global__ void __launch_bounds__(256) render_adjoint_kernel(const float* __rest
             const float dm = measured[i];
             const float r = ts - dm;
             if (dm > 0.f && !(fabsf(r) > g.max_residual)) {
+                // Huber: weight min(1, delta / |r|) (iteratively reweighted least squares),
+                // so w r = clamp(r, -delta, delta) is the loss's derivative; the loss term
+                // is 2 rho(r) = r^2 inside the threshold, 2 delta |r| - delta^2 outside
+                const float ar = fabsf(r);
+                const bool out = g.huber > 0.f && ar > g.huber;
+                const float w = out ? g.huber / ar : 1.f;
                 int q = 0;
 #pragma unroll
                 for (int a = 0; a < 6; ++a)
 #pragma unroll
-                    for (int b = a; b < 6; ++b) acc[q++] = jt[a] * jt[b];
+                    for (int b = a; b < 6; ++b) acc[q++] = w * (jt[a] * jt[b]);
 #pragma unroll
-                for (int a = 0; a < 6; ++a) acc[21 + a] = jt[a] * r;
+                for (int a = 0; a < 6; ++a) acc[21 + a] = jt[a] * (w * r);
                 acc[27] = 1.f;
-                acc[28] = r * r;
+                acc[28] = out ? g.huber * (2.f * ar - g.huber) : r * r;
             }
         }
     }
@@ -386,6 +393,7 @@ bool make_geom(const kf_render_desc* d, const float T[16], kf::RenderGeom& g)
     const double steps = std::ceil(((double)d->t_far - d->t_near) / d->step) + 1.0;
     g.max_steps = steps > 1e6 ? 1000000 : (int)steps;
     g.max_residual = INFINITY;
+    g.huber = 0.f;
     return true;
 }
 
@@ -417,10 +425,20 @@ extern "C" kf_status kf_render_depth_normal_equations(const kf_render_desc* d, c
                                                       const float* measured_depth, float max_residual, double sums[29],
                                                       void* stream)
 {
+    return kf_render_depth_normal_equations_huber(d, tsdf, T, measured_depth, max_residual, 0.f, sums, stream);
+}
+
+extern "C" kf_status kf_render_depth_normal_equations_huber(const kf_render_desc* d, const float* tsdf,
+                                                            const float T[16], const float* measured_depth,
+                                                            float max_residual, float huber_delta, double sums[29],
+                                                            void* stream)
+{
     kf::RenderGeom g;
-    if (!tsdf || !measured_depth || !sums || !make_geom(d, T, g) || std::isnan(max_residual))
+    if (!tsdf || !measured_depth || !sums || !make_geom(d, T, g) || std::isnan(max_residual) ||
+        !(huber_delta >= 0.f))
         return KF_ERR_INVALID_ARGUMENT;
     g.max_residual = max_residual > 0.f ? max_residual : INFINITY;
+    g.huber = huber_delta;
     const int n = g.H * g.W, blocks = (n + 255) / 256;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     float* partials = nullptr;

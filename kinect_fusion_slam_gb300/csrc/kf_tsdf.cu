@@ -538,6 +538,42 @@ __global__ void __launch_bounds__(kIntTx* kIntTy, 5) integrate_batch_kernel(cons
                               t / (nbx * nby));
 }
 
+// every scene's integration as a persistent launch: blocks take boxes one at a time from
+// one counter over all scenes' boxes (scene s owns boxes [int_start of s, int_start of
+// s + 1)), so the scenes' live boxes share the SMs without blocks for the boxes smaller
+// grids do not have; counter: two unsigneds, zero between launches (the last block to
+// leave resets them)
+template <class Vol, bool FIRST>
+__global__ void __launch_bounds__(kIntTx* kIntTy, 5) integrate_batch_persist_kernel(
+    const SceneDev* __restrict__ scenes, int n_scenes, int zchunk, unsigned total, unsigned* counter)
+{
+    wait_for_producer();
+    __shared__ unsigned s_box;
+    const bool lead = threadIdx.x == 0 && threadIdx.y == 0;
+    for (;;) {
+        __syncthreads();  // the previous box is done with s_box and the cull flag
+        if (lead) s_box = atomicAdd(counter, 1u);
+        __syncthreads();
+        const unsigned box = s_box;
+        if (box >= total) {
+            if (lead && atomicAdd(counter + 1, 1u) == gridDim.x - 1) {
+                counter[0] = 0u;
+                counter[1] = 0u;
+            }
+            return;
+        }
+        int s = 0;
+        while (s + 1 < n_scenes && box >= (unsigned)scenes[s + 1].int_start) ++s;
+        const SceneDev& d = scenes[s];
+        const Grid& g = d.grid;
+        const int nbx = (g.dx + kIntTx - 1) / kIntTx, nby = (g.dy + kIntTy - 1) / kIntTy;
+        const int t = (int)(box - (unsigned)d.int_start);
+        const Vol vol = scene_volume(d, (Vol*)nullptr);
+        integrate_box<Vol, FIRST>(vol, d.tab, d.st, g, scene_params(d, zchunk), t % nbx, (t / nbx) % nby,
+                                  t / (nbx * nby));
+    }
+}
+
 // Ray_Box_Intersection, voxel_traversal.cu:4-73
 __device__ __forceinline__ float slab_entry(bool& inside, float3 d, float3 lo, float3 hi, float3 o)
 {
@@ -1086,6 +1122,28 @@ void launch_integrate_batch(const SceneDev* scenes, int n_scenes, int max_pixels
             launch_pdl(integrate_batch_kernel<VolF32, true>, grid, block, 0, s, scenes, zchunk);
         else
             launch_pdl(integrate_batch_kernel<VolF32, false>, grid, block, 0, s, scenes, zchunk);
+    }
+}
+
+void launch_integrate_batch_persistent(const SceneDev* scenes, int n_scenes, int max_pixels, unsigned total_boxes,
+                                       int zchunk, bool f16, bool first, int blocks, unsigned* counter, cudaStream_t s)
+{
+    launch_pdl(integrate_prep_batch_kernel, dim3((max_pixels / 64 + 7) / 8 + 1, n_scenes), dim3(256), 0, s, scenes);
+    const dim3 grid(blocks), block(kIntTx, kIntTy);
+    if (f16) {
+        if (first)
+            launch_pdl(integrate_batch_persist_kernel<VolF16, true>, grid, block, 0, s, scenes, n_scenes, zchunk,
+                       total_boxes, counter);
+        else
+            launch_pdl(integrate_batch_persist_kernel<VolF16, false>, grid, block, 0, s, scenes, n_scenes, zchunk,
+                       total_boxes, counter);
+    } else {
+        if (first)
+            launch_pdl(integrate_batch_persist_kernel<VolF32, true>, grid, block, 0, s, scenes, n_scenes, zchunk,
+                       total_boxes, counter);
+        else
+            launch_pdl(integrate_batch_persist_kernel<VolF32, false>, grid, block, 0, s, scenes, n_scenes, zchunk,
+                       total_boxes, counter);
     }
 }
 

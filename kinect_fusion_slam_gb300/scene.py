@@ -305,3 +305,28 @@ def sequence(cfg: SceneConfig | str, frames: int | None = None) -> Sequence:
     if frames is not None:
         cfg = SceneConfig(**{**cfg.__dict__, "frames": frames})
     return Sequence(cfg, make_scene(cfg), trajectory(cfg), cfg.camera.K_reference())
+
+
+def _render_task(task):
+    cfg, k = task
+    seq = sequence(cfg)
+    return render_depth_mm(cfg, seq.scene, seq.poses[k], k)
+
+
+def render_sequences(cfgs: list[SceneConfig], frames: int, processes: int | None = None) -> list[np.ndarray]:
+    """The first `frames` depth frames of each scene, (frames, H, W) uint16 per scene,
+    rendered by a pool of spawned processes (the renderer is CPU numpy; spawned workers
+    start fresh interpreters, so a caller that has already initialised CUDA is safe).
+    Identical to Sequence.depths, frame for frame."""
+    import multiprocessing as mp
+    import os
+
+    cfgs = [SceneConfig(**{**c.__dict__, "frames": max(frames, c.frames)}) for c in cfgs]
+    tasks = [(c, k) for c in cfgs for k in range(frames)]
+    n = processes or min(len(tasks), os.cpu_count() or 1)
+    if n <= 1:
+        out = [_render_task(t) for t in tasks]
+    else:
+        with mp.get_context("spawn").Pool(n) as pool:
+            out = pool.map(_render_task, tasks, chunksize=max(1, len(tasks) // (4 * n)))
+    return [np.stack(out[i * frames:(i + 1) * frames]) for i in range(len(cfgs))]

@@ -38,11 +38,15 @@ def _intrinsics(h, seq):
     h.set_intrinsics(K[0, 0], K[1, 1], K[0, 2], K[1, 2])
 
 
-@pytest.mark.parametrize("levels,tune", [(1, False), (3, True)])
-def test_batch_matches_scenes_run_alone(levels, tune):
+@pytest.mark.parametrize("levels,tune,persistent", [(1, False, False), (3, True, False), (1, False, True),
+                                                   (3, True, True)])
+def test_batch_matches_scenes_run_alone(levels, tune, persistent):
+    """persistent: integration and the ICP group pass spread over one fixed grid for all
+    scenes (kf_batch_set_forms) instead of one row of blocks per scene."""
     data = _scenes()
     configs = [_config(seq, d, levels) for seq, d in data]
     b = kf.Batch(configs)
+    b.set_forms(persistent, persistent)
     singles = [kf.Handle(c) for c in configs]
     for (seq, _), hb, hs in zip(data, b.scenes, singles):
         _intrinsics(hb, seq)
