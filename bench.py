@@ -614,11 +614,15 @@ def run_differentiation(args) -> dict:
     torch.cuda.synchronize()
     n = len(w.starts)
 
-    # the pose gradient against central differences, on pixels whose bracket is stable
-    def stable(depth):
-        f = (depth.double() - w.desc.t_near) / w.desc.step
-        f = f - torch.floor(f)
-        return (depth > 0) & (f > 0.05) & (f < 0.95)
+    # the pose gradient against central differences, on pixels whose crossing stays
+    # between the same two samples of the march in every evaluation
+    def bracket(depth):
+        return torch.floor((depth.double() - w.desc.t_near) / w.desc.step)
+
+    def stable(depth, b0):
+        b = bracket(depth)
+        f = (depth.double() - w.desc.t_near) / w.desc.step - b
+        return (depth > 0) & (f > 0.05) & (f < 0.95) & (b == b0)
 
     eps = np.array([1e-4] * 3 + [0.1] * 3)
     rel = []
@@ -626,8 +630,9 @@ def run_differentiation(args) -> dict:
         T, tg = w.starts[k], targets[k]
         poses = [T] + [diff.se3_exp(sg * eps[q] * np.eye(6)[q]) @ T for q in range(6) for sg in (1, -1)]
         mask = tg > 0
+        b0 = bracket(diff.render(w.desc, w.tsdf, T)[0])
         for P in poses:
-            mask &= stable(diff.render(w.desc, w.tsdf, P)[0])
+            mask &= stable(diff.render(w.desc, w.tsdf, P)[0], b0)
         mask = mask.double()
 
         def loss(P):
@@ -637,6 +642,28 @@ def run_differentiation(args) -> dict:
         _, g6 = diff.render_backward(w.desc, w.tsdf, T, (psi * mask).float(), None, want_tsdf=False)
         fd = np.array([(loss(poses[1 + 2 * q]) - loss(poses[2 + 2 * q])) / (2 * eps[q]) for q in range(6)])
         rel.append(float(np.max(np.abs(g6.double().cpu().numpy() - fd)) / np.abs(fd).max()))
+
+    # the depth Jacobian against the point-to-plane ICP row -[x cross m, m]/(m.r) on
+    # locally flat pixels (rendered normal within 3 degrees over 9x9) at the first pose
+    T = w.poses[0]
+    depth, normal = diff.render(w.desc, w.tsdf, T)
+    nrm, dep = normal.double().cpu().numpy(), depth.cpu().numpy()
+    Ki = np.linalg.inv(np.asarray(w.K, np.float64))
+    p2p = []
+    for v in range(40, dep.shape[0] - 40, 11):
+        for u in range(40, dep.shape[1] - 40, 14):
+            if dep[v, u] <= 0 or not np.all(dep[v - 4:v + 5, u - 4:u + 5] > 0):
+                continue
+            m = nrm[v, u] / np.linalg.norm(nrm[v, u])
+            if (nrm[v - 4:v + 5, u - 4:u + 5] @ m).min() < np.cos(np.radians(3.0)):
+                continue
+            g1 = torch.zeros_like(depth)
+            g1[v, u] = 1.0
+            _, gp = diff.render_backward(w.desc, w.tsdf, T, g1, None, want_tsdf=False)
+            r = T[:3, :3] @ (Ki @ np.array([u + 1.0, v + 1.0, 1.0]))
+            x = T[:3, 3] + float(dep[v, u]) * r
+            want = -np.concatenate([np.cross(x, m), m]) / float(m @ r)
+            p2p.append(float(np.linalg.norm(gp.double().cpu().numpy() - want) / np.linalg.norm(want)))
 
     steps = 50
     ref, icp = [], []
@@ -665,6 +692,8 @@ def run_differentiation(args) -> dict:
             "observed_voxels": observed, "render_ms": e[0].elapsed_time(e[1]) / n,
             "adjoint_ms": e[1].elapsed_time(e[2]) / n,
             "pose_gradient_vs_central_differences": {"step": "1e-4 rad, 0.1 mm", "max_rel_error": max(rel)},
+            "depth_jacobian_vs_point_to_plane_row": {"pixels": len(p2p), "median_rel_diff": float(np.median(p2p)),
+                                                     "p90_rel_diff": float(np.percentile(p2p, 90))},
             "start_error_median_mm": float(np.median(start_err[:, 0])),
             "start_error_median_deg": float(np.median(start_err[:, 1])),
             "refinement": {"steps": steps, "ms_per_step": 1000.0 * t_ref / (n * steps), **summary(ref)},

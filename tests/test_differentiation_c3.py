@@ -33,13 +33,21 @@ def room():
     w.close()
 
 
-def _stable(w, depth, margin=0.05):
-    """Pixels whose crossing lies away from the march's sample points, so a small pose
-    change keeps the same bracketing samples (the linear crossing between two samples is
-    continuous only while the bracket stays)."""
-    f = (depth.double() - w.desc.t_near) / w.desc.step
-    f = f - torch.floor(f)
-    return (depth > 0) & (f > margin) & (f < 1 - margin)
+def _bracket(w, depth):
+    """The index of the march's sample before each pixel's crossing."""
+    return torch.floor((depth.double() - w.desc.t_near) / w.desc.step)
+
+
+def _stable(w, depth, margin=0.05, bracket=None):
+    """Pixels whose crossing lies away from the march's sample points (and, given a
+    reference, between the same two samples as there): the rendered depth -- the linear
+    crossing between two samples -- is a smooth function of the pose and the voxels only
+    while the bracket stays, and a ray whose first crossing moves to another surface
+    (an occlusion edge) jumps."""
+    b = _bracket(w, depth)
+    f = (depth.double() - w.desc.t_near) / w.desc.step - b
+    ok = (depth > 0) & (f > margin) & (f < 1 - margin)
+    return ok if bracket is None else ok & (b == bracket)
 
 
 def _loss(w, T, target, mask):
@@ -55,8 +63,9 @@ def test_pose_gradient_against_central_differences(room, k):
     eps = np.array([H_ROT] * 3 + [H_TRANS] * 3)
     poses = [T] + [diff.se3_exp(s * eps[q] * np.eye(6)[q]) @ T for q in range(6) for s in (1, -1)]
     mask = (target > 0)
+    b0 = _bracket(w, diff.render(w.desc, w.tsdf, T)[0])
     for P in poses:
-        mask &= _stable(w, diff.render(w.desc, w.tsdf, P)[0])
+        mask &= _stable(w, diff.render(w.desc, w.tsdf, P)[0], bracket=b0)
     mask = mask.double()
     assert mask.sum() > 50_000
     depth, _ = diff.render(w.desc, w.tsdf, T)
@@ -73,6 +82,7 @@ def test_voxel_gradient_against_central_differences(room):
     w = room
     T, target = w.starts[10], w.targets[10]
     depth, _ = diff.render(w.desc, w.tsdf, T)
+    b0 = _bracket(w, depth)
     mask = ((target > 0) & _stable(w, depth, 0.02)).double()
     _, psi = diff.huber(depth.double() - target, DELTA)
     gt, _ = diff.render_backward(w.desc, w.tsdf, T, (psi * mask).float(), None)
@@ -84,8 +94,8 @@ def test_voxel_gradient_against_central_differences(room):
         tp, tm = w.tsdf.clone(), w.tsdf.clone()
         tp.view(-1)[idx] += eps
         tm.view(-1)[idx] -= eps
-        m = mask * _stable(w, diff.render(w.desc, tp, T)[0], 0.02).double() * \
-            _stable(w, diff.render(w.desc, tm, T)[0], 0.02).double()
+        m = mask * _stable(w, diff.render(w.desc, tp, T)[0], 0.02, b0).double() * \
+            _stable(w, diff.render(w.desc, tm, T)[0], 0.02, b0).double()
         g_an, _ = diff.render_backward(w.desc, w.tsdf, T, (psi * m).float(), None)
         lp = float((diff.huber(diff.render(w.desc, tp, T)[0].double() - target, DELTA)[0] * m).sum())
         lm = float((diff.huber(diff.render(w.desc, tm, T)[0].double() - target, DELTA)[0] * m).sum())
@@ -97,27 +107,29 @@ def test_voxel_gradient_against_central_differences(room):
 
 
 def test_depth_jacobian_is_the_point_to_plane_row_on_flat_faces(room):
-    """On the room's flat faces (rendered normal within 1 degree of an axis over a 9x9
-    window) the depth Jacobian is -[x cross m, m]/(m.r) with m that axis."""
+    """On locally flat parts of the fused surfaces (the rendered normal within 3 degrees
+    over a 9x9 window) the depth Jacobian of a pixel is close to the point-to-plane ICP
+    row -[x cross m, m]/(m.r), m the surface normal at the crossing.  The two agree
+    exactly where the TSDF is affine (tests/test_differentiation.py, planar TSDF); the
+    fused volume of noisy depth is not affine within a cell, and the rendered crossing
+    interpolates between two samples whose gradients differ from the crossing's, so the
+    check here is on the distribution of the relative difference over the pixels."""
     w = room
     T = w.poses[0]
     depth, normal = diff.render(w.desc, w.tsdf, T)
-    n = normal.cpu().numpy()
+    n = normal.double().cpu().numpy()
     dep = depth.cpu().numpy()
     Hh, Ww = dep.shape
     Ki = np.linalg.inv(np.asarray(w.K, np.float64))
     R, o = T[:3, :3], T[:3, 3]
-    cos1 = np.cos(np.radians(1.0))
-    checked = 0
-    for v in range(40, Hh - 40, 47):
-        for u in range(40, Ww - 40, 61):
-            if dep[v, u] <= 0:
+    cos3 = np.cos(np.radians(3.0))
+    checked, rel = 0, []
+    for v in range(40, Hh - 40, 11):
+        for u in range(40, Ww - 40, 14):
+            if dep[v, u] <= 0 or not np.all(dep[v - 4:v + 5, u - 4:u + 5] > 0):
                 continue
-            axis = np.argmax(np.abs(n[v, u]))
-            m = np.zeros(3)
-            m[axis] = np.sign(n[v, u, axis])
-            win = n[v - 4:v + 5, u - 4:u + 5] @ m
-            if win.min() < cos1:
+            m = n[v, u] / np.linalg.norm(n[v, u])
+            if (n[v - 4:v + 5, u - 4:u + 5] @ m).min() < cos3:
                 continue
             g1 = torch.zeros_like(depth)
             g1[v, u] = 1.0
@@ -126,9 +138,13 @@ def test_depth_jacobian_is_the_point_to_plane_row_on_flat_faces(room):
             x = o + float(dep[v, u]) * r
             want = -np.concatenate([np.cross(x, m), m]) / float(m @ r)
             got = gp.double().cpu().numpy()
-            assert np.allclose(got, want, rtol=0.05, atol=0.05 * np.abs(want).max()), (v, u, got, want)
+            rel.append(float(np.linalg.norm(got - want) / np.linalg.norm(want)))
             checked += 1
-    assert checked >= 8, checked
+    rel = np.array(rel)
+    print(f"point-to-plane rows at {checked} pixels: relative difference median {np.median(rel):.4f}, "
+          f"90th percentile {np.percentile(rel, 90):.4f}, max {rel.max():.4f}")
+    assert checked >= 20, checked
+    assert np.median(rel) <= 0.03 and np.percentile(rel, 90) <= 0.10
 
 
 def test_refinement_beside_icp_from_the_64_starts(room):
