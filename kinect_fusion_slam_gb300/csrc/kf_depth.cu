@@ -125,10 +125,12 @@ constexpr int kBilTx = 32, kBilTy = 8, kBilMaxR = 7;
 // bilateral_filtering.cu:3-47 with the interior bound tightened to y <= H-1-r,
 // x <= W-1-r so the 7x7 window never leaves the image (the reference's `<= H - r`
 // reads one row/column past it); pixels outside the interior are 0, as the reference's
-// zero-initialised output buffer leaves them.  The reference writes the result over
-// depth_image_next, which Estimate_Sensor_Pose then reads as the vertices' z
-// (kinfu_pipeline.cpp:141-160); with vmap given, its z takes the filtered depth too (x, y,
-// the mask and the normals stay those of the unfiltered depth, as in the reference).
+// zero-initialised output buffer leaves them.  In the frame loop the filter sits at the
+// reference's commented-out call site (kinfu_pipeline.cpp:141-145), after the vertex map.
+// That call writes bilateral_output, which nothing reads; this library instead feeds the
+// result forward as if written over depth_image_next, which Estimate_Sensor_Pose reads as
+// the vertices' z (kinfu_pipeline.cpp:146-160): with vmap given, its z takes the filtered
+// depth too (x, y, the mask and the normals stay those of the unfiltered depth).
 __global__ void __launch_bounds__(kBilTx* kBilTy) bilateral_kernel(const float* __restrict__ depth,
                                                                     float* __restrict__ out,
                                                                     const float* __restrict__ spatial, int r,

@@ -681,8 +681,9 @@ static void incoming(kfo_pipeline* p, const uint16_t* raw, const float* filtered
     float* c = p->cur6.data();
     kfo_vertex_normal(H, W, p->depth.data(), p->Ki, c, c + HW, c + 3 * HW, c + 4 * HW, c + 5 * HW, p->mask.data());
     if (p->bilateral) {
-        /* Bilateral_Filtering writes over depth_image_next, which ICP then reads as the
-         * vertices' z and integration and the ray cast as the depth */
+        /* the filtered depth is fed forward as if written over depth_image_next (the
+         * reference's commented-out call writes bilateral_output, which nothing reads):
+         * ICP reads it as the vertices' z, integration and the ray cast as the depth */
         p->filtered.assign(HW, 0.f);
         if (filtered_in)
             std::memcpy(p->filtered.data(), filtered_in, sizeof(float) * HW);
