@@ -524,6 +524,37 @@ __device__ __forceinline__ void add_terms_fused(float (&v)[kIcpVals], const floa
 
 // Group pass: one warp per 64-pixel group writes the group's 28 sums (27 terms and
 // the correspondence count) and whether the group has a correspondence.
+// Sums each of the 28 values over the warp; lane l < 28 returns the sum of value l.  A
+// butterfly in which every exchange halves the values a lane carries: 16 + 8 + 4 + 2 + 1
+// shuffles in all, where a sum per value and level takes 28 per level.  At the exchange
+// of width w a lane adds, for each value it keeps, its own partial at position p and its
+// partner's at p ^ w, so every value is summed by the pairs (t, t + w), w = 16, 8, 4, 2,
+// 1 -- the reference's shared-memory tree (sensor_pose_estimation.cu:225-245) after its
+// stride-32 step, with each addition's operands in either order (addition commutes).
+__device__ __forceinline__ float warp_sum_transposed(const float (&v)[kIcpVals])
+{
+    const int lane = threadIdx.x & 31;
+    float a[16];
+    {
+        const bool up = lane & 16;
+#pragma unroll
+        for (int k = 0; k < 16; ++k) {
+            const float lo = v[k], hi = k + 16 < kIcpVals ? v[k + 16] : 0.f;
+            a[k] = (up ? hi : lo) + __shfl_xor_sync(0xffffffffu, up ? lo : hi, 16);
+        }
+    }
+#pragma unroll
+    for (int w = 8; w >= 1; w >>= 1) {
+        const bool up = lane & w;
+#pragma unroll
+        for (int k = 0; k < w; ++k) {
+            const float lo = a[k], hi = a[k + w];
+            a[k] = (up ? hi : lo) + __shfl_xor_sync(0xffffffffu, up ? lo : hi, w);
+        }
+    }
+    return a[0];
+}
+
 template <int MODE>
 __device__ __forceinline__ void group_sums(int grp, int lane, const float4* __restrict__ vmap,
                                            const float4* __restrict__ nmap, const float4* __restrict__ pv,
@@ -552,16 +583,10 @@ __device__ __forceinline__ void group_sums(int grp, int lane, const float4* __re
 #pragma unroll
         for (int k = 0; k < kIcpVals; ++k) v[k] = v[k] + w[k];  // sdata[t] += sdata[t + 32]
     }
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1)
-#pragma unroll
-        for (int k = 0; k < kIcpVals; ++k) v[k] = v[k] + __shfl_down_sync(0xffffffffu, v[k], off);
-    if (lane == 0) {
-        flags[grp] = v[kIcpVals - 1] != 0.f ? 1 : 0;
-        float4* dst = reinterpret_cast<float4*>(partials + (size_t)grp * kIcpVals);
-#pragma unroll
-        for (int q = 0; q < kIcpVals / 4; ++q) dst[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
-    }
+    // the rest of the tree, strides 16 .. 1, for all 28 values at once; lane k keeps value k
+    const float vs = warp_sum_transposed(v);
+    if (lane < kIcpVals) partials[(size_t)grp * kIcpVals + lane] = vs;
+    if (lane == kIcpVals - 1) flags[grp] = vs != 0.f ? 1 : 0;
 }
 
 template <int MODE>
@@ -958,33 +983,6 @@ __device__ __forceinline__ double take(const long long* digits, int k, bool flag
 }
 
 }  // namespace fix
-
-// Sums each of the 28 values over the warp; lane l < 28 returns the sum of value l.  A
-// butterfly in which every exchange halves the values a lane carries: 16 + 8 + 4 + 2 + 1
-// shuffles in all, where a sum per value and level takes 28 per level.
-__device__ __forceinline__ float warp_sum_transposed(const float (&v)[kIcpVals])
-{
-    const int lane = threadIdx.x & 31;
-    float a[16];
-    {
-        const bool up = lane & 16;
-#pragma unroll
-        for (int k = 0; k < 16; ++k) {
-            const float lo = v[k], hi = k + 16 < kIcpVals ? v[k + 16] : 0.f;
-            a[k] = (up ? hi : lo) + __shfl_xor_sync(0xffffffffu, up ? lo : hi, 16);
-        }
-    }
-#pragma unroll
-    for (int w = 8; w >= 1; w >>= 1) {
-        const bool up = lane & w;
-#pragma unroll
-        for (int k = 0; k < w; ++k) {
-            const float lo = a[k], hi = a[k + w];
-            a[k] = (up ? hi : lo) + __shfl_xor_sync(0xffffffffu, up ? lo : hi, w);
-        }
-    }
-    return a[0];
-}
 
 template <int MODE>
 __global__ void __launch_bounds__(kPreciseWarps * 32, 32 / kPreciseWarps) icp_precise_kernel(

@@ -702,22 +702,20 @@ __device__ __forceinline__ void trace(const View& vol, float X, float Y, float D
     constexpr int kAhead = 4;
     int ali = li;
     float3 atm = tm;
+    // The axis choice as predicates and selects, with no branch: lanes of a warp step
+    // along different axes, and a three-way branch per step diverged (61.6 -> 58.0 us
+    // per c1 frame without it).
     auto lead_step = [&]() -> int {
         const bool xy = atm.x < atm.y, xz = atm.x < atm.z, yz = atm.y < atm.z;
-        int d;
-        if (xy && xz) {
-            rx -= 1;
-            atm.x = atm.x + td.x;
-            d = dlx;
-        } else if (!xy && yz) {
-            ry -= 1;
-            atm.y = atm.y + td.y;
-            d = dly;
-        } else {
-            rz -= 1;
-            atm.z = atm.z + td.z;
-            d = dlz;
-        }
+        const bool px = xy && xz, py = !xy && yz, pz = !px && !py;
+        rx -= (int)px;
+        ry -= (int)py;
+        rz -= (int)pz;
+        const float nx = atm.x + td.x, ny = atm.y + td.y, nz = atm.z + td.z;
+        atm.x = px ? nx : atm.x;
+        atm.y = py ? ny : atm.y;
+        atm.z = pz ? nz : atm.z;
+        const int d = px ? dlx : (py ? dly : dlz);
         ali += d;
         return d;
     };
