@@ -524,6 +524,16 @@ __device__ __forceinline__ void add_terms_fused(float (&v)[kIcpVals], const floa
 
 // Group pass: one warp per 64-pixel group writes the group's 28 sums (27 terms and
 // the correspondence count) and whether the group has a correspondence.
+// The group sums (plain form) are stored quad-interleaved: for each quad of four
+// consecutive groups, term k's four values are adjacent (float4 k of the quad), so the
+// in-order reduction reads four groups of a term with one 16-byte load.
+constexpr int kQuad = 4;
+constexpr int kQuadFloats = kQuad * kIcpVals;  // 112 floats = 448 bytes per quad
+__device__ __forceinline__ size_t partial_index(int grp, int term)
+{
+    return (size_t)(grp >> 2) * kQuadFloats + term * kQuad + (grp & 3);
+}
+
 // Sums each of the 28 values over the warp; lane l < 28 returns the sum of value l.  A
 // butterfly in which every exchange halves the values a lane carries: 16 + 8 + 4 + 2 + 1
 // shuffles in all, where a sum per value and level takes 28 per level.  At the exchange
@@ -585,7 +595,7 @@ __device__ __forceinline__ void group_sums(int grp, int lane, const float4* __re
     }
     // the rest of the tree, strides 16 .. 1, for all 28 values at once; lane k keeps value k
     const float vs = warp_sum_transposed(v);
-    if (lane < kIcpVals) partials[(size_t)grp * kIcpVals + lane] = vs;
+    if (lane < kIcpVals) partials[partial_index(grp, lane)] = vs;
     if (lane == kIcpVals - 1) flags[grp] = vs != 0.f ? 1 : 0;
 }
 
@@ -664,16 +674,17 @@ __global__ void __launch_bounds__(WARPS * 32) icp_group_batch_persist_kernel(con
 // order by the bulk-copy engine (cp.async.bulk into a ring of kBuffers chunks with
 // mbarrier completion; kBuffers - 1 copies stay in flight) while the warp adds them:
 // lane k keeps the running sum of term k.  The additions run as one software pipeline
-// over batches of kBatch groups -- the next batch's shared-memory loads are issued
-// before the current batch's additions, across chunk boundaries too -- so the serial
-// part is the FADD chain itself.  Empty groups sum to +0 and are added like the rest
-// (exact).  Then the warp solves and updates the pose (MODE 0) or writes the sums
-// (MODE 1).
+// over batches of kBatchQ quads (16 groups) -- the next batch's shared-memory loads are
+// issued before the current batch's additions, across chunk boundaries too -- so the
+// serial part is the FADD chain itself; a lane reads a quad's four values of its term
+// with one 16-byte load and adds them in group order.  Empty groups sum to +0 and are
+// added like the rest (exact).  Then the warp solves and updates the pose (MODE 0) or
+// writes the sums (MODE 1).
 constexpr int kChunkGroups = 512;                               // 512 x 112 B = 56 KB
 constexpr int kBuffers = 2;
-constexpr int kBatch = 16;
-constexpr int kBatchesPerChunk = kChunkGroups / kBatch;
-static_assert(kChunkGroups % (2 * kBatch) == 0, "a chunk is an even number of batches");
+constexpr int kBatchQ = 4;                                      // quads per batch
+constexpr int kBatchesPerChunk = kChunkGroups / (kQuad * kBatchQ);
+static_assert(kChunkGroups % (2 * kQuad * kBatchQ) == 0, "a chunk is an even number of batches");
 constexpr unsigned kChunkBytes = kChunkGroups * kIcpVals * 4u;  // multiple of 16
 
 __device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
@@ -727,7 +738,11 @@ __device__ __forceinline__ void solve_body(const float* __restrict__ partials, i
         it = st->iter;
     }
     const int nchunks = (ngroups + kChunkGroups - 1) / kChunkGroups;
-    auto chunk_bytes = [&](int c) { return (unsigned)(min(kChunkGroups, ngroups - c * kChunkGroups) * kIcpVals * 4); };
+    // whole quads: a partial last quad is copied whole (the buffer holds whole quads; the
+    // values past ngroups are not added)
+    auto chunk_bytes = [&](int c) {
+        return (unsigned)((min(kChunkGroups, ngroups - c * kChunkGroups) + kQuad - 1) / kQuad * kQuadFloats * 4);
+    };
     if (lane == 0) {
         for (int k = 0; k < kBuffers; ++k)
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&bars[k])) : "memory");
@@ -739,51 +754,58 @@ __device__ __forceinline__ void solve_body(const float* __restrict__ partials, i
     __syncwarp();
     // chunks issued so far (uniform over the warp), and the chunk whose wait gave up
     int issued = min(kBuffers, nchunks), failed_at = 0;
-    // lanes 28..31 read term 27's column too (in bounds) and discard it
+    // lanes 28..31 read term 27's values too (in bounds) and discard them
     const int term = lane < kIcpVals ? lane : kIcpVals - 1;
-    auto slot_ptr = [&](int c) { return buf + (c % kBuffers) * kChunkGroups * kIcpVals + term; };
+    // quad q of chunk c's slot, this lane's term: float4 q * kIcpVals + term
+    auto slot_ptr = [&](int c) {
+        return reinterpret_cast<const float4*>(buf + (c % kBuffers) * kChunkGroups * kIcpVals) + term;
+    };
     float sum = 0.f;
+    auto add4 = [&](const float4& q) {
+        sum = sum + q.x;
+        sum = sum + q.y;
+        sum = sum + q.z;
+        sum = sum + q.w;
+    };
     bool ok = nchunks == 0 || bar_wait(&bars[0], 0, limit);
     const int full = ngroups / kChunkGroups;  // chunks of exactly kChunkGroups groups
-    float va[kBatch], vb[kBatch];
+    float4 va[kBatchQ], vb[kBatchQ];
     if (ok && full > 0) {
-        const float* p = slot_ptr(0);
+        const float4* p = slot_ptr(0);
 #pragma unroll
-        for (int q = 0; q < kBatch; ++q) va[q] = p[q * kIcpVals];
+        for (int q = 0; q < kBatchQ; ++q) va[q] = p[q * kIcpVals];
     }
     for (int c = 0; c < full && ok; ++c) {
         // batches 0..kBatchesPerChunk-1 of chunk c; va holds batch 0 on entry.  The next
         // batch's loads are issued before the current batch's additions.
-        const float* p = slot_ptr(c);
-        // each load is issued between two dependent additions, in the issue slots the
-        // FADD latency leaves free
+        const float4* p = slot_ptr(c);
         for (int i = 0; i < kBatchesPerChunk - 2; i += 2) {
 #pragma unroll
-            for (int q = 0; q < kBatch; ++q) {
-                vb[q] = p[((i + 1) * kBatch + q) * kIcpVals];
-                sum = sum + va[q];
+            for (int q = 0; q < kBatchQ; ++q) {
+                vb[q] = p[((i + 1) * kBatchQ + q) * kIcpVals];
+                add4(va[q]);
             }
 #pragma unroll
-            for (int q = 0; q < kBatch; ++q) {
-                va[q] = p[((i + 2) * kBatch + q) * kIcpVals];
-                sum = sum + vb[q];
+            for (int q = 0; q < kBatchQ; ++q) {
+                va[q] = p[((i + 2) * kBatchQ + q) * kIcpVals];
+                add4(vb[q]);
             }
         }
 #pragma unroll
-        for (int q = 0; q < kBatch; ++q) {
-            vb[q] = p[((kBatchesPerChunk - 1) * kBatch + q) * kIcpVals];
-            sum = sum + va[q];
+        for (int q = 0; q < kBatchQ; ++q) {
+            vb[q] = p[((kBatchesPerChunk - 1) * kBatchQ + q) * kIcpVals];
+            add4(va[q]);
         }
         // open the next full chunk before the last batch's additions
         if (c + 1 < full) {
             ok = bar_wait(&bars[(c + 1) % kBuffers], ((c + 1) / kBuffers) & 1, limit);
             if (!ok) failed_at = c + 1;
-            const float* pn = slot_ptr(c + 1);
+            const float4* pn = slot_ptr(c + 1);
 #pragma unroll
-            for (int q = 0; q < kBatch; ++q) va[q] = ok ? pn[q * kIcpVals] : 0.f;
+            for (int q = 0; q < kBatchQ; ++q) va[q] = ok ? pn[q * kIcpVals] : make_float4(0.f, 0.f, 0.f, 0.f);
         }
 #pragma unroll
-        for (int q = 0; q < kBatch; ++q) sum = sum + vb[q];
+        for (int q = 0; q < kBatchQ; ++q) add4(vb[q]);
         // every group of chunk c is added: its slot goes back to the copy engine
         __syncwarp();
         if (ok && c + kBuffers < nchunks) {
@@ -798,22 +820,29 @@ __device__ __forceinline__ void solve_body(const float* __restrict__ partials, i
         }
     }
     if (ok && full < nchunks) {
-        // the last, partial chunk, in batches without prefetch
+        // the last, partial chunk: whole quads, then the groups of a partial last quad
         if (full > 0) {
             ok = bar_wait(&bars[full % kBuffers], (full / kBuffers) & 1, limit);
             if (!ok) failed_at = full;
         }
         if (ok) {
-            const float* p = slot_ptr(full);
+            const float4* p = slot_ptr(full);
             const int cnt = ngroups - full * kChunkGroups;
+            const int nq = cnt / kQuad, rem = cnt % kQuad;
             int r = 0;
-            for (; r + kBatch <= cnt; r += kBatch) {
+            for (; r + kBatchQ <= nq; r += kBatchQ) {
 #pragma unroll
-                for (int q = 0; q < kBatch; ++q) va[q] = p[(r + q) * kIcpVals];
+                for (int q = 0; q < kBatchQ; ++q) va[q] = p[(r + q) * kIcpVals];
 #pragma unroll
-                for (int q = 0; q < kBatch; ++q) sum = sum + va[q];
+                for (int q = 0; q < kBatchQ; ++q) add4(va[q]);
             }
-            for (; r < cnt; ++r) sum = sum + p[r * kIcpVals];
+            for (; r < nq; ++r) add4(p[r * kIcpVals]);
+            if (rem) {
+                const float4 t = p[nq * kIcpVals];
+                sum = sum + t.x;
+                if (rem > 1) sum = sum + t.y;
+                if (rem > 2) sum = sum + t.z;
+            }
         }
     }
     if (!ok) {
@@ -1132,7 +1161,7 @@ size_t icp_fixacc_words() { return (size_t)fix::kDigits * fix::kFixReplicas; }
 size_t icp_scratch_floats(int H, int W)
 {
     const size_t a = (size_t)2 * blocks_for(H, W) * kIcpVals;
-    const size_t b = (size_t)icp_groups(H, W) * kIcpVals;
+    const size_t b = (size_t)((icp_groups(H, W) + kQuad - 1) / kQuad) * kQuadFloats;  // whole quads
     return a > b ? a : b;
 }
 
