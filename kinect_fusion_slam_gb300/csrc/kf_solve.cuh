@@ -200,34 +200,27 @@ static __device__ __noinline__ float mat4_entry_f64(const float* a, const float*
 // lower triangle holding A on entry and the factor (reciprocal diagonal) on return;
 // x: 6 shared floats, b on entry, the solution on return when the factorisation
 // succeeds and untouched when a pivot is below FLT_EPSILON (then false is returned).
-// The factor is computed column by column -- column j's pivot by lane j, its other
-// entries by lanes j+1..5 -- with each entry's terms in chol6's order.
+// Lane r (r + 1) / 2 + c holds entry (r, c) of the lower triangle as a running sum.
+// The factor is computed column by column: column j's pivot and then its other entries
+// are rounded from their sums, and every entry right of column j subtracts its term of
+// column j at once (right-looking), so each entry's terms still come in chol6's order,
+// k = 0, 1, ..., c - 1.  The substitutions likewise keep one row per lane: once x_k is
+// final, every later row subtracts its term of x_k, each row's terms in chol6's order.
+// Shared L keeps A's value in an entry until the entry is final (the FP64 fallbacks
+// read both).
 __device__ __forceinline__ bool warp_chol6(float* L, float* x, int* fail)
 {
     const int lane = threadIdx.x & 31;
+    const bool ent = lane < 21;
+    const int r = (lane >= 1) + (lane >= 3) + (lane >= 6) + (lane >= 10) + (lane >= 15);
+    const int c = ent ? lane - r * (r + 1) / 2 : 0;
+    const int rr = ent ? r : 0;
+    ff::Acc acc;
+    acc.init(ent ? L[rr * 6 + c] : 0.f);
     if (lane == 0) *fail = 0;
     __syncwarp();
     for (int j = 0; j < 6; ++j) {
-        const int row = lane < 6 ? lane : 5;
-        const bool active = lane >= j && lane < 6;
-        ff::Acc acc;
-        acc.init(active ? L[row * 6 + j] : 0.f);
-        if (active) {
-            for (int k = 0; k < j; ++k) {
-                // the pivot subtracts the exact square of L[j][k], the other entries the
-                // float product L[row][k] * L[j][k]; one instruction stream for both
-                const float t = L[row * 6 + k];
-                const float u = lane == j ? t : L[j * 6 + k];
-                const float p = t * u;
-                const float pe = lane == j ? fmaf(t, u, -p) : 0.f;
-                float s, e;
-                ff::two_sum(acc.h, -p, s, e);
-                acc.h = s;
-                acc.l = (acc.l + e) - pe;
-                acc.m = acc.m + fabsf(p);
-            }
-        }
-        if (lane == j) {
+        if (ent && rr == j && c == j) {
             const float H = acc.h + acc.l, E = acc.bound();
             bool decided = false;
             if (H * 0.999f - 2.f * E >= FLT_EPSILON) {
@@ -244,31 +237,51 @@ __device__ __forceinline__ bool warp_chol6(float* L, float* x, int* fail)
         }
         __syncwarp();
         if (*fail) return false;
-        if (lane > j && lane < 6) {
+        if (ent && c == j && rr > j) {
             const float piv = L[j * 6 + j];
             float v;
-            if (!ff::mul_round_f32(acc.h, acc.l, acc.bound(), piv, v)) v = ff::offdiag_f64(L, lane, j);
-            L[lane * 6 + j] = v;
+            if (!ff::mul_round_f32(acc.h, acc.l, acc.bound(), piv, v)) v = ff::offdiag_f64(L, rr, j);
+            L[rr * 6 + j] = v;
         }
         __syncwarp();
+        if (ent && c > j) {
+            // the diagonal subtracts the exact square of L[r][j], the other entries the
+            // float product L[r][j] * L[c][j]
+            const float t = L[rr * 6 + j];
+            const float u = rr == c ? t : L[c * 6 + j];
+            const float pr = t * u;
+            const float pe = rr == c ? fmaf(t, u, -pr) : 0.f;
+            float sum, e;
+            ff::two_sum(acc.h, -pr, sum, e);
+            acc.h = sum;
+            acc.l = (acc.l + e) - pe;
+            acc.m = acc.m + fabsf(pr);
+        }
     }
-    if (lane == 0) {
-        for (int i = 0; i < 6; ++i) {
-            ff::Acc acc;
-            acc.init(x[i]);
-            for (int k = 0; k < i; ++k) acc.add(-(L[i * 6 + k] * x[k]));
+    // forward: row i = lane i
+    const bool row = lane < 6;
+    ff::Acc ax;
+    ax.init(row ? x[lane] : 0.f);
+    for (int k = 0; k < 6; ++k) {
+        if (lane == k) {
             float v;
-            if (!ff::mul_round_f32(acc.h, acc.l, acc.bound(), L[i * 6 + i], v)) v = ff::subst_f64(L, x, i, 0);
-            x[i] = v;
+            if (!ff::mul_round_f32(ax.h, ax.l, ax.bound(), L[k * 6 + k], v)) v = ff::subst_f64(L, x, k, 0);
+            x[k] = v;
         }
-        for (int i = 5; i >= 0; --i) {
-            ff::Acc acc;
-            acc.init(x[i]);
-            for (int k = 5; k > i; --k) acc.add(-(L[k * 6 + i] * x[k]));
+        __syncwarp();
+        if (row && lane > k) ax.add(-(L[lane * 6 + k] * x[k]));
+    }
+    // backward
+    ax.init(row ? x[lane] : 0.f);
+    __syncwarp();
+    for (int k = 5; k >= 0; --k) {
+        if (lane == k) {
             float v;
-            if (!ff::mul_round_f32(acc.h, acc.l, acc.bound(), L[i * 6 + i], v)) v = ff::subst_f64(L, x, i, 1);
-            x[i] = v;
+            if (!ff::mul_round_f32(ax.h, ax.l, ax.bound(), L[k * 6 + k], v)) v = ff::subst_f64(L, x, k, 1);
+            x[k] = v;
         }
+        __syncwarp();
+        if (row && lane < k) ax.add(-(L[k * 6 + lane] * x[k]));
     }
     __syncwarp();
     return true;
