@@ -101,6 +101,9 @@ __global__ void __launch_bounds__(256) vertex_kernel(const uint16_t* __restrict_
                                                      float4* __restrict__ vmap, float4* __restrict__ nmap, Camera cam,
                                                      float dmin, float dmax, State* st, int init_icp, int normals)
 {
+    // the next kernel (launched with launch_pdl) may be scheduled now; it waits for this
+    // one before reading anything it writes
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     vertex_body<RAW>(blockIdx.x * blockDim.x + threadIdx.x, raw, depth, vmap, nmap, cam, dmin, dmax, st, init_icp,
                      normals);
 }

@@ -565,12 +565,13 @@ __device__ __forceinline__ float warp_sum_transposed(const float (&v)[kIcpVals])
     return a[0];
 }
 
+// group_sums with the lane's two vertices and normals already loaded (load_pair)
 template <int MODE>
-__device__ __forceinline__ void group_sums(int grp, int lane, const float4* __restrict__ vmap,
-                                           const float4* __restrict__ nmap, const float4* __restrict__ pv,
-                                           const float4* __restrict__ pn, const Camera& cam, const IcpParams& prm,
-                                           const float* sF, const float* sT, float* __restrict__ partials,
-                                           int* __restrict__ flags, int32_t* __restrict__ pair)
+__device__ __forceinline__ void group_sums_from(int grp, int lane, const float4 (&vx)[2], const float4 (&nx)[2],
+                                                const float4* __restrict__ pv, const float4* __restrict__ pn,
+                                                const Camera& cam, const IcpParams& prm, const float* sF,
+                                                const float* sT, float* __restrict__ partials,
+                                                int* __restrict__ flags, int32_t* __restrict__ pair)
 {
     const int n = cam.H * cam.W;
     float v[kIcpVals];
@@ -579,7 +580,7 @@ __device__ __forceinline__ void group_sums(int grp, int lane, const float4* __re
     bool ok[2];
     float a[2][6], b[2];
     int j[2];
-    associate_pair(grp * 64 + lane, n, vmap, nmap, pv, pn, cam, sF, sT, prm.dist, prm.angle_deg, ok, a, b, j);
+    associate_pair_from(vx, nx, pv, pn, cam, sF, sT, prm.dist, prm.angle_deg, ok, a, b, j);
     if (MODE == 1 && pair) {
         if (grp * 64 + lane < n) pair[grp * 64 + lane] = ok[0] ? j[0] : -1;
         if (grp * 64 + 32 + lane < n) pair[grp * 64 + 32 + lane] = ok[1] ? j[1] : -1;
@@ -600,21 +601,43 @@ __device__ __forceinline__ void group_sums(int grp, int lane, const float4* __re
 }
 
 template <int MODE>
+__device__ __forceinline__ void group_sums(int grp, int lane, const float4* __restrict__ vmap,
+                                           const float4* __restrict__ nmap, const float4* __restrict__ pv,
+                                           const float4* __restrict__ pn, const Camera& cam, const IcpParams& prm,
+                                           const float* sF, const float* sT, float* __restrict__ partials,
+                                           int* __restrict__ flags, int32_t* __restrict__ pair)
+{
+    float4 vx[2], nx[2];
+    load_pair(grp * 64 + lane, cam.H * cam.W, vmap, nmap, vx, nx);
+    group_sums_from<MODE>(grp, lane, vx, nx, pv, pn, cam, prm, sF, sT, partials, flags, pair);
+}
+
+template <int MODE>
 __global__ void __launch_bounds__(kExactWarps * 32, 4) icp_group_kernel(
     const float4* __restrict__ vmap, const float4* __restrict__ nmap, const float4* __restrict__ pv,
     const float4* __restrict__ pn, Camera cam, IcpParams prm, const float* Fsrc, const float* Tsrc,
-    float* __restrict__ partials, int* __restrict__ flags, int ngroups, int32_t* __restrict__ pair)
+    float* __restrict__ partials, int* __restrict__ flags, int ngroups, int32_t* __restrict__ pair, int prefetch)
 {
+    // one group per warp (the grid covers the groups)
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int grp = blockIdx.x * kExactWarps + warp;
+    const int n = cam.H * cam.W;
+    // The vertex and normal maps are written before the frame's first ICP pass and never
+    // by a pass, so after a pass (prefetch) they are loaded before waiting for it: the
+    // first round of loads overlaps the previous pass's reduction and solve.
+    float4 vx[2], nx[2];
+    if (prefetch) load_pair(grp * 64 + lane, n, vmap, nmap, vx, nx);
     wait_for_producer();
+    // the solve pass may be scheduled now: it waits for this pass before reading its sums
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    if (!prefetch) load_pair(grp * 64 + lane, n, vmap, nmap, vx, nx);
     __shared__ float sF[16], sT[16];
     if (threadIdx.x < 16) {
         sF[threadIdx.x] = Fsrc[threadIdx.x];
         sT[threadIdx.x] = Tsrc[threadIdx.x];
     }
     __syncthreads();
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int grp = blockIdx.x * kExactWarps + warp; grp < ngroups; grp += gridDim.x * kExactWarps)
-        group_sums<MODE>(grp, lane, vmap, nmap, pv, pn, cam, prm, sF, sT, partials, flags, pair);
+    if (grp < ngroups) group_sums_from<MODE>(grp, lane, vx, nx, pv, pn, cam, prm, sF, sT, partials, flags, pair);
 }
 
 // the group pass of every scene of a batch at pyramid level `level`; WARPS warps per
@@ -1110,6 +1133,9 @@ __global__ void __launch_bounds__(32, 1) icp_solve_kernel(const float* __restric
                                                         IcpParams prm, float* sums_out)
 {
     wait_for_producer();
+    // the next pass may be scheduled now and load what no pass writes; it waits for this
+    // one before reading the pose
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     solve_body<MODE>(partials, ngroups, st, prm, sums_out);
 }
 
@@ -1197,7 +1223,7 @@ void launch_icp_iteration(const float4* vmap, const float4* nmap, const float4* 
         const int ng = icp_groups(cam.H, cam.W);
         ensure_solve_smem(ng);
         launch_pdl(icp_group_kernel<0>, dim3(exact_blocks(cam.H, cam.W)), dim3(kExactWarps * 32), 0, s, vmap, nmap, pv,
-                   pn, cam, prm, state_F(st), state_T(st), partials, list, ng, (int32_t*)nullptr);
+                   pn, cam, prm, state_F(st), state_T(st), partials, list, ng, (int32_t*)nullptr, after_pass ? 1 : 0);
         launch_pdl(icp_solve_kernel<0>, dim3(1), dim3(32), solve_smem_bytes(ng), s, (const float*)partials, ng, st,
                    prm, (float*)nullptr);
     } else if (prm.precise) {
@@ -1220,7 +1246,7 @@ void launch_icp_associate(const float4* vmap, const float4* nmap, const float4* 
         const int ng = icp_groups(cam.H, cam.W);
         ensure_solve_smem(ng);
         launch_pdl(icp_group_kernel<1>, dim3(exact_blocks(cam.H, cam.W)), dim3(kExactWarps * 32), 0, s, vmap, nmap, pv,
-                   pn, cam, prm, F, T, partials, list, ng, pair);
+                   pn, cam, prm, F, T, partials, list, ng, pair, 0);
         launch_pdl(icp_solve_kernel<1>, dim3(1), dim3(32), solve_smem_bytes(ng), s, (const float*)partials, ng, st,
                    prm, sums_out);
     } else if (prm.precise) {

@@ -165,6 +165,8 @@ __global__ void __launch_bounds__(256) integrate_prep_kernel(const float* __rest
                                                              Camera cam, State* st)
 {
     wait_for_producer();
+    // integration may be scheduled now; it waits for this kernel before reading the table
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     const int tiles = bound_tiles_x(cam.W) * ((cam.H + kBoundTile - 1) / kBoundTile);
     const int tile = blockIdx.x * 8 + (threadIdx.x >> 5);
     if (tile < tiles) integrate_prep_tile(tile, threadIdx.x & 31, depth, tab, cam, st);
@@ -498,6 +500,9 @@ __global__ void __launch_bounds__(kIntTx* kIntTy, 5) integrate_kernel(Vol vol, c
                                                                    IntegrateParams p)
 {
     wait_for_producer();
+    // the ray cast may be scheduled once every box has started; it waits for this kernel
+    // before reading the volume
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     integrate_box<Vol, FIRST>(vol, tab, st, g, p, blockIdx.x, blockIdx.y, blockIdx.z);
 }
 
