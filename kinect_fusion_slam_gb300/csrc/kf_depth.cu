@@ -28,52 +28,39 @@ __device__ __forceinline__ float ingest(uint16_t raw, float dmin, float dmax)
     return (d >= dmin && d <= dmax) ? d : 0.f;
 }
 
-// raw_vertices.cu:3-51.  One thread per pixel; the mask is kept in vmap.w.
-template <bool RAW>
-__device__ __forceinline__ void vertex_body(int i, const uint16_t* __restrict__ raw, float* __restrict__ depth,
-                                            float4* __restrict__ vmap, float4* __restrict__ nmap, const Camera& cam,
-                                            float dmin, float dmax, State* st, int init_icp, int normals)
+// Frame start of Estimate_Sensor_Pose (sensor_pose_estimation.cu:255-259, 343), by one
+// warp: T_prev^-1 = inv4(T), F = mat4(T_prev^-1, T).  The previous frame's integration
+// inverted the same pose when T has not changed since, so its inverse is copied;
+// otherwise the warp inverts T.
+__device__ __forceinline__ void icp_frame_setup(State* st, int lane)
+{
+    const bool same = __all_sync(0xffffffffu, lane >= 16 || __float_as_uint(st->T[lane]) ==
+                                                                __float_as_uint(st->Tinv_src[lane]));
+    if (same) {
+        if (lane < 16) st->Tprev_inv[lane] = st->Tinv[lane];
+    } else {
+        inv4_warp(st->T, st->Tprev_inv);
+    }
+    __syncwarp();
+    if (lane < 16) {
+        st->F[lane] = mat4_at(st->Tprev_inv, st->T, lane);
+        st->Td[lane] = (double)st->T[lane];
+    }
+    if (lane == 0) st->iter = 0;
+}
+
+// raw_vertices.cu:3-51 for pixel (row, col) with depth d and its lower and right
+// neighbours' depths dd, dr (read only inside the image); the mask is kept in vmap.w.
+__device__ __forceinline__ void vertex_at(int row, int col, float d, float dd, float dr, float4* __restrict__ vmap,
+                                          float4* __restrict__ nmap, const Camera& cam)
 {
     const int H = cam.H, W = cam.W;
-    if (init_icp && i < 32) {
-        // Frame start of Estimate_Sensor_Pose (sensor_pose_estimation.cu:255-259, 343),
-        // by the first warp: T_prev^-1 = inv4(T), F = mat4(T_prev^-1, T).  The previous
-        // frame's integration inverted the same pose when T has not changed since, so
-        // its inverse is copied; otherwise the warp inverts T.
-        const int lane = i;
-        const bool same = __all_sync(0xffffffffu, lane >= 16 || __float_as_uint(st->T[lane]) ==
-                                                                    __float_as_uint(st->Tinv_src[lane]));
-        if (same) {
-            if (lane < 16) st->Tprev_inv[lane] = st->Tinv[lane];
-        } else {
-            inv4_warp(st->T, st->Tprev_inv);
-        }
-        __syncwarp();
-        if (lane < 16) {
-            st->F[lane] = mat4_at(st->Tprev_inv, st->T, lane);
-            st->Td[lane] = (double)st->T[lane];
-        }
-        if (lane == 0) st->iter = 0;
-    }
-    if (i >= H * W) return;
-    const int row = i / W, col = i % W;
-    float d;
-    if (RAW) {
-        d = ingest(raw[i], dmin, dmax);
-        depth[i] = d;
-    } else {
-        d = depth[i];
-    }
-    if (!normals) return;
+    const int i = row * W + col;
     float4 v = make_float4(0.f, 0.f, d, 0.f);
     float4 n = make_float4(0.f, 0.f, 0.f, 0.f);
     if (d != 0 && row != H - 1 && col != W - 1) {
         v.w = 1.f;
-        const int down = (row + 1) * W + col;
-        const int right = row * W + col + 1;
-        const float dd = RAW ? ingest(raw[down], dmin, dmax) : depth[down];
-        const float dr = RAW ? ingest(raw[right], dmin, dmax) : depth[right];
-        if (down > 0 && right > 0 && dd != 0 && dr != 0) {
+        if (dd != 0 && dr != 0) {
             const float* Ki = cam.Ki;
             const float X = (float)(col + 1), Y = (float)(row + 1);
             const float px = d * (Ki[0] * X + Ki[1] * Y + Ki[2]);
@@ -96,16 +83,66 @@ __device__ __forceinline__ void vertex_body(int i, const uint16_t* __restrict__ 
     nmap[i] = n;
 }
 
+// One thread per pixel (batched scenes): the depth and its neighbours from global memory.
 template <bool RAW>
-__global__ void __launch_bounds__(256) vertex_kernel(const uint16_t* __restrict__ raw, float* __restrict__ depth,
-                                                     float4* __restrict__ vmap, float4* __restrict__ nmap, Camera cam,
-                                                     float dmin, float dmax, State* st, int init_icp, int normals)
+__device__ __forceinline__ void vertex_body(int i, const uint16_t* __restrict__ raw, float* __restrict__ depth,
+                                            float4* __restrict__ vmap, float4* __restrict__ nmap, const Camera& cam,
+                                            float dmin, float dmax, State* st, int init_icp, int normals)
+{
+    const int H = cam.H, W = cam.W;
+    if (init_icp && i < 32) icp_frame_setup(st, i);
+    if (i >= H * W) return;
+    const int row = i / W, col = i % W;
+    float d;
+    if (RAW) {
+        d = ingest(raw[i], dmin, dmax);
+        depth[i] = d;
+    } else {
+        d = depth[i];
+    }
+    if (!normals) return;
+    float dd = 0.f, dr = 0.f;
+    if (d != 0 && row != H - 1 && col != W - 1) {
+        const int down = (row + 1) * W + col, right = row * W + col + 1;
+        dd = RAW ? ingest(raw[down], dmin, dmax) : depth[down];
+        dr = RAW ? ingest(raw[right], dmin, dmax) : depth[right];
+    }
+    vertex_at(row, col, d, dd, dr, vmap, nmap, cam);
+}
+
+// One handle's image: 32x8-pixel tiles whose depths (ingested from the raw frame, or the
+// given depth) are staged in shared memory with the row below and the column to the
+// right, so each pixel's two neighbours come from the tile.  The grid's first warp also
+// prepares the frame's ICP (init_icp).
+constexpr int kVtx = 32, kVty = 8;
+
+template <bool RAW>
+__global__ void __launch_bounds__(kVtx* kVty) vertex_kernel(const uint16_t* __restrict__ raw, float* __restrict__ depth,
+                                                            float4* __restrict__ vmap, float4* __restrict__ nmap,
+                                                            Camera cam, float dmin, float dmax, State* st, int init_icp,
+                                                            int normals)
 {
     // the next kernel (launched with launch_pdl) may be scheduled now; it waits for this
     // one before reading anything it writes
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-    vertex_body<RAW>(blockIdx.x * blockDim.x + threadIdx.x, raw, depth, vmap, nmap, cam, dmin, dmax, st, init_icp,
-                     normals);
+    __shared__ float sd[kVty + 1][kVtx + 1];
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int H = cam.H, W = cam.W;
+    const int col = blockIdx.x * kVtx + tx, row = blockIdx.y * kVty + ty;
+    if (init_icp && blockIdx.x == 0 && blockIdx.y == 0 && ty == 0) icp_frame_setup(st, tx);
+    const auto load = [&](int r, int c) { return RAW ? ingest(raw[r * W + c], dmin, dmax) : depth[r * W + c]; };
+    const bool in = row < H && col < W;
+    float d = 0.f;
+    if (in) {
+        d = load(row, col);
+        if (RAW) depth[row * W + col] = d;
+    }
+    if (!normals) return;  // the same in every thread
+    sd[ty][tx] = d;
+    if (ty == kVty - 1) sd[kVty][tx] = row + 1 < H && col < W ? load(row + 1, col) : 0.f;
+    if (tx == kVtx - 1) sd[ty][kVtx] = row < H && col + 1 < W ? load(row, col + 1) : 0.f;
+    __syncthreads();
+    if (in) vertex_at(row, col, d, sd[ty + 1][tx], sd[ty][tx + 1], vmap, nmap, cam);
 }
 
 // every scene of a batch: level 0 from the raw depth (with the ICP set-up), or level l
@@ -292,13 +329,12 @@ void launch_fill_nan_half2(__half2* p, size_t n, cudaStream_t s)
 void launch_vertex(const uint16_t* raw, float* depth, float4* vmap, float4* nmap, const Camera& cam, float dmin,
                    float dmax, State* st, bool init_icp, bool compute_normals, cudaStream_t s)
 {
-    const int n = cam.H * cam.W;
-    const int blocks = (n + 255) / 256;
+    const dim3 grid((cam.W + kVtx - 1) / kVtx, (cam.H + kVty - 1) / kVty), block(kVtx, kVty);
     if (raw)
-        vertex_kernel<true><<<blocks, 256, 0, s>>>(raw, depth, vmap, nmap, cam, dmin, dmax, st, init_icp ? 1 : 0,
+        vertex_kernel<true><<<grid, block, 0, s>>>(raw, depth, vmap, nmap, cam, dmin, dmax, st, init_icp ? 1 : 0,
                                                    compute_normals ? 1 : 0);
     else
-        vertex_kernel<false><<<blocks, 256, 0, s>>>(raw, depth, vmap, nmap, cam, dmin, dmax, st, init_icp ? 1 : 0,
+        vertex_kernel<false><<<grid, block, 0, s>>>(raw, depth, vmap, nmap, cam, dmin, dmax, st, init_icp ? 1 : 0,
                                                     compute_normals ? 1 : 0);
 }
 
