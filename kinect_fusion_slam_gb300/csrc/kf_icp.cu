@@ -170,17 +170,6 @@ __device__ __forceinline__ void associate_pair_from(const float4 (&v)[2], const 
         if (ok[h]) ok[h] = assoc_finish(g[h], nn[h], q[h], m[h], T, dist_th, ang_th, a[h], b[h]);
 }
 
-__device__ __forceinline__ void associate_pair(int i0, int n, const float4* __restrict__ vmap,
-                                               const float4* __restrict__ nmap, const float4* __restrict__ pv,
-                                               const float4* __restrict__ pn, const Camera& cam, const float* F,
-                                               const float* T, float dist_th, float ang_th, bool (&ok)[2],
-                                               float (&a)[2][6], float (&b)[2], int (&j)[2])
-{
-    float4 v[2], nn[2];
-    load_pair(i0, n, vmap, nmap, v, nn);
-    associate_pair_from(v, nn, pv, pn, cam, F, T, dist_th, ang_th, ok, a, b, j);
-}
-
 // The precision form's association: the gates, matched pixel, row a and residual b of
 // assoc_project + assoc_finish (sensor_pose_estimation.cu:20-131), in FP32 with the
 // arithmetic arranged for fewer instructions -- products fused into FMAs, the
