@@ -359,11 +359,10 @@ __device__ void finish_precise_pair(State* st, const IcpParams& prm, const doubl
     const int t = threadIdx.x, lane = t & 31;
     const float tp = t < 16 ? st->Tprev_inv[t] : 0.f;
     const double td = t < 16 ? st->Td[t] : 0.0;
+    const int it = st->iter;
     const auto entry = [S](int r, int c) { return c == 6 ? S[r] : S[tri(min(r, c), max(r, c))]; };
     const bool ok = pair_gj6_f64(entry, t, gj_buf, gj_x, 1);
     if (t >= 32) return;
-    const int it = st->iter;
-    if (lane < kIcpVals) st->sums[lane] = (float)S[lane];
     // the increment (omega, t) in every lane; where A is not positive definite the
     // reference applies b as it stands, or the identity in that fail mode
     double x[6];
@@ -393,6 +392,9 @@ __device__ void finish_precise_pair(State* st, const IcpParams& prm, const doubl
         st->F[lane] = f;
         if (it < kMaxIcpIters) st->Tlog[it][lane] = Tf[lane];
     }
+    // the statistics after the pose (their conversions would queue on the FP64 pipe
+    // ahead of the composition)
+    if (lane < kIcpVals) st->sums[lane] = (float)S[lane];
     if (lane == 0) {
         if (it < kMaxIcpIters) {
             st->ncorr[it] = (int32_t)S[kIcpVals - 1];
@@ -1003,10 +1005,9 @@ __device__ __forceinline__ double take(const long long* digits, int k, bool flag
     unsigned long long lhi = (unsigned long long)(t & M);  // L = lhi 2^64 + llo
     unsigned long long llo = (w1 << 32) | w0;
     long long top = d3 + (t >> 32);
-    double sign = 1.0;
-    if (top < 0) {
+    const bool neg = top < 0;
+    if (neg) {
         // |V| = (-top - 1) 2^96 + (2^96 - L), or -top 2^96 when L = 0
-        sign = -1.0;
         if (lhi == 0ull && llo == 0ull) {
             top = -top;
         } else {
@@ -1016,11 +1017,45 @@ __device__ __forceinline__ double take(const long long* digits, int k, bool flag
             lhi = ((1ull << 32) - lhi - borrow) & 0xffffffffull;
         }
     }
-    // non-negative terms from the top: a relative error of a few ulps, no cancellation
+    if (((unsigned long long)top >> 32) == 0ull) {
+        // |V| < 2^128 (every sum of this pipeline): |V| 2^-48 rounded to the nearest
+        // double by integer arithmetic on the 128-bit magnitude h 2^64 + l -- normalise,
+        // keep 53 bits, round half to even -- so the conversion uses no FP64 instruction
+        const unsigned long long h = ((unsigned long long)top << 32) | lhi, l = llo;
+        if ((h | l) == 0ull) return 0.0;
+        const int lz = h ? __clzll((long long)h) : 64 + __clzll((long long)l);
+        unsigned long long nh;
+        unsigned long long nl;
+        if (lz >= 64) {
+            nh = l << (lz - 64);
+            nl = 0ull;
+        } else if (lz == 0) {
+            nh = h;
+            nl = l;
+        } else {
+            nh = (h << lz) | (l >> (64 - lz));
+            nl = l << lz;
+        }
+        unsigned long long mant = nh >> 11;  // 53 bits, the leading one at bit 52
+        int e = 127 - lz;                    // the leading bit's exponent in |V|
+        const bool half = ((nh >> 10) & 1ull) != 0ull;
+        const bool sticky = (nh & 0x3ffull) != 0ull || nl != 0ull;
+        if (half && (sticky || (mant & 1ull))) {
+            ++mant;
+            if (mant >> 53) {
+                mant >>= 1;
+                ++e;
+            }
+        }
+        const unsigned long long bits = ((unsigned long long)(e - 48 + 1023) << 52) | (mant & 0xfffffffffffffull) |
+                                        (neg ? (1ull << 63) : 0ull);
+        return __longlong_as_double((long long)bits);
+    }
+    // beyond 2^128: non-negative terms from the top, a relative error of a few ulps
     double v = (double)top * 0x1p96;
     v += (double)lhi * 0x1p64;
     v += (double)llo;
-    return sign * v * 0x1p-48;
+    return (neg ? -v : v) * 0x1p-48;
 }
 
 }  // namespace fix

@@ -302,7 +302,7 @@ __device__ __forceinline__ float mat4_entry(const float* a, const float* b, int 
 }
 
 // Division by the pivot in the Gauss-Jordan steps: q = a / p for p > 0 in
-// [2^-1000, 2^1000].  y0 = rcp.approx.ftz.f64(p) has a relative error e0 = 1 - p y0
+// [2^-999, 2^1000).  y0 = rcp.approx.ftz.f64(p) has a relative error e0 = 1 - p y0
 // of about 2^-20 (kf_selftest_solve6 checks the solves built on this); then
 // a / p = a y0 / (1 - e0) = a y0 (1 + e0 + e0^2 + e0^3 + ...), and the first three terms
 // leave a relative error e0^3 ~ 2^-60, below FP64 rounding.  a y0 and e0 are independent,
@@ -410,7 +410,9 @@ __device__ __forceinline__ bool pair_gj6_f64(const Entry& entry, int t, double (
         pair_bar(bar_id);
         const double p = M[j][j];
         const int ep = (__double2hiint(p) >> 20) & 0x7ff;
-        pd = pd && p > 0.0;
+        // p > 0 by its sign bit: a zero, subnormal or non-finite p (ep 0 or 0x7ff) sets
+        // bad and is decided again below (comparisons run on the FP64 pipe here)
+        pd = pd && __double2hiint(p) >= 0;
         bad = bad || ep == 0 || ep == 0x7ff;
         const double ps = scale_by_pivot(p, ep, bad);  // in [1, 2)
         // rows i != j: a <- p' a - m' q on the live columns c > j, a <- p' a elsewhere
@@ -425,8 +427,10 @@ __device__ __forceinline__ bool pair_gj6_f64(const Entry& entry, int t, double (
     const double d = __shfl_sync(0xffffffffu, a, act ? (l / 7) * 7 + r : 0);
     bool inf = false;
     if (act && c == 6) {
-        const double xr = (d > 0x1p-1000 && d < 0x1p1000) ? div_pivot(a, d) : a / d;
-        inf = !isfinite(xr);
+        // d in [2^-999, 2^1000) by its sign and exponent field
+        const int dh = __double2hiint(d), ed = (dh >> 20) & 0x7ff;
+        const double xr = (dh >= 0 && ed > 23 && ed < 2023) ? div_pivot(a, d) : a / d;
+        inf = ((__double2hiint(xr) >> 20) & 0x7ff) == 0x7ff;
         x[r] = xr;
     }
     // out of range anywhere: neither the decision nor x can be trusted (a subnormal
