@@ -394,9 +394,10 @@ def run_form(args, dist, form, cfg, frames, order, fresh, stream, **extra):
     kpf = h.kernels_per_frame()
     n_fresh = sum(fresh[1 + args.warmup:n_total])
     # a restart: reset (two NaN fills or one for the FP16 pair, the state reset) and
-    # InitialProcessing (vertex map, integration prep, integration, ray cast)
+    # InitialProcessing (vertex map, integration prep, box marks, mark list, integration,
+    # ray cast)
     reset_kernels = 2 if FORMS[form]["tsdf"] == "f16" else 3
-    launches = kpf * (args.steps - n_fresh) + (4 + reset_kernels) * n_fresh
+    launches = kpf * (args.steps - n_fresh) + (6 + reset_kernels) * n_fresh
 
     # per-stage device time with CUDA events recorded inside each frame's graph
     # (incoming frames only: InitialProcessing has no ICP stage)

@@ -221,10 +221,11 @@ void enq_integrate(kf_handle* h, bool first)
 {
     launch_integrate_prep(h->d_depth, h->d_tab, h->cam, h->d_state, h->stream);
     if (h->d_vol16)
-        launch_integrate_f16(h->d_vol16, h->d_tab, h->d_state, h->grid, h->cam, h->skip_from, first, h->stream);
+        launch_integrate_f16(h->d_vol16, h->d_tab, h->d_state, h->grid, h->cam, h->skip_from, first, h->d_mark,
+                             h->stream);
     else
         launch_integrate_f32(h->d_tsdf, h->d_weight, h->d_tab, h->d_state, h->grid, h->cam, h->skip_from, first,
-                             h->stream);
+                             h->d_mark, h->stream);
 }
 
 void enq_raycast(kf_handle* h, int32_t* hit)
@@ -401,6 +402,9 @@ kf_status allocate(kf_handle* h)
     KF_TRY(dalloc(h, &h->d_groups, (size_t)icp_groups(h->cam.H, h->cam.W)));
     KF_TRY(dalloc(h, &h->d_tiles, 2));
     KF_CUDA(h, cudaMemset(h->d_tiles, 0, 2 * sizeof(unsigned)));
+    // box marks, then the list of marked boxes
+    KF_TRY(dalloc(h, &h->d_mark, 2 * (size_t)integrate_boxes(h->grid)));
+    KF_CUDA(h, cudaMemset(h->d_mark, 0, 2 * sizeof(unsigned) * (size_t)integrate_boxes(h->grid)));
     KF_TRY(dalloc(h, &h->d_mats, 64));
     KF_TRY(dalloc(h, &h->d_spatial, 15 * 15));
     h->d_depth_l[0] = h->d_depth;
@@ -479,7 +483,7 @@ void free_all(kf_handle* h)
     void* dev[] = {h->d_raw, h->d_raw_alt, h->d_depth, h->d_depth_tmp, h->d_vmap, h->d_nmap, h->d_pv, h->d_pn, h->d_hit,
                    h->d_pair, h->d_tab, h->d_tsdf, h->d_weight, h->d_vol16, h->d_state, h->d_partials, h->d_groups,
                    h->d_fixacc,
-                   h->d_tiles, h->d_mats,
+                   h->d_tiles, h->d_mark, h->d_mats,
                    h->d_spatial};
     for (void* p : dev)
         if (p) cudaFree(p);
@@ -593,6 +597,7 @@ kf_status kf_create(const kf_config* cfg, kf_handle** out)
     if (s == KF_OK) {
         icp_prepare(h->cam.H, h->cam.W);
         raycast_blocks();
+        integrate_blocks();
     }
     if (s == KF_OK && cfg->bilateral) s = upload_spatial(h);
     if (s == KF_OK) s = reset_state(h);
@@ -1335,12 +1340,12 @@ kf_status kf_kernels_per_frame(kf_handle* h, int* n)
     if (!h || !n) return KF_ERR_INVALID_ARGUMENT;
     // vertex, [bilateral], ICP iterations (in the reference summation order a 64-pixel
     // group pass and a one-warp reduce-and-solve pass; the precision form and the tree
-    // reduction one pass each), integration prep, integration, ray cast
+    // reduction one pass each), integration prep, box marks, mark list, integration, ray cast
     const int per_iteration =
         (h->cfg.icp_reduction == KF_REDUCE_REFERENCE_ORDER && h->cfg.solve_mode != KF_SOLVE_PRECISE) ? 2 : 1;
     int iterations = 0;
     for (int l = 0; l < h->cfg.icp_levels; ++l) iterations += h->cfg.icp_iterations[l];
-    *n = 1 + (h->cfg.bilateral ? 1 : 0) + 3 * (h->cfg.icp_levels - 1) + per_iteration * iterations + 3;
+    *n = 1 + (h->cfg.bilateral ? 1 : 0) + 3 * (h->cfg.icp_levels - 1) + per_iteration * iterations + 5;
     return KF_OK;
 }
 

@@ -44,6 +44,7 @@ struct kf_handle {
     float* d_partials = nullptr;
     int* d_groups = nullptr;  // ICP group flags / compacted group list
     unsigned* d_tiles = nullptr;  // ray-cast tile counter
+    unsigned* d_mark = nullptr;   // integration box marks and mark list (2 x integrate_boxes words)
     float* d_mats = nullptr;  // F, T (debug association input) + sums output
     float* d_spatial = nullptr;
     // ICP pyramid: level 0 aliases the buffers above; levels 1.. are half size each

@@ -64,12 +64,15 @@ float depth_band_eps(const Camera& cam);
 // largest |K^-1 (u, v, 1)| over the image (with a margin)
 float ray_norm_max(const Camera& cam);
 // projective TSDF update (projective_tsdf.cu:5-140) in 32x8x16 voxel boxes, skipping
-// boxes and column segments that provably hold no updated voxel; skip_from = first
-// z-fastest index the reference's float guard never reaches
+// the boxes that provably hold no updated voxel: a marking pass over the depth tiles
+// marks (mark[box] = 1) every box a tile's pixels can update, a compaction lists the
+// marked boxes after the marks and clears the marks, and a persistent pass updates the
+// listed boxes; mark holds 2 x integrate_boxes words, zero before the first call;
+// skip_from = first z-fastest index the reference's float guard never reaches
 void launch_integrate_f32(float* tsdf, float* weight, const float2* tab, const State* st, const Grid& g,
-                          const Camera& cam, long long skip_from, bool first, cudaStream_t s);
+                          const Camera& cam, long long skip_from, bool first, unsigned* mark, cudaStream_t s);
 void launch_integrate_f16(__half2* vol, const float2* tab, const State* st, const Grid& g, const Camera& cam,
-                          long long skip_from, bool first, cudaStream_t s);
+                          long long skip_from, bool first, unsigned* mark, cudaStream_t s);
 
 // Amanatides-Woo ray cast (voxel_traversal.cu:75-424); hit may be nullptr; tile_counter
 // points to two device unsigneds, zero before the first launch, with which the persistent
@@ -80,6 +83,8 @@ void launch_raycast_f16(const __half2* vol, const float* depth, float4* pv, floa
                         const Camera& cam, const Grid& g, const State* st, unsigned* tile_counter, cudaStream_t s);
 // once per device, outside any stream capture: sizes the persistent ray-cast grid
 int raycast_blocks();
+// the same for the persistent integration pass
+int integrate_blocks();
 
 // st->c_flip from the device's own double acos (single thread, once per handle)
 void launch_calibrate(State* st, cudaStream_t s);
@@ -105,6 +110,8 @@ void launch_icp_iteration_batch(const SceneDev* scenes, int n_scenes, int max_gr
 void launch_integrate_batch(const SceneDev* scenes, int n_scenes, int max_pixels, int max_tiles, int zchunk, bool f16,
                             bool first, cudaStream_t s);
 int integrate_tiles(const Grid& g, int zchunk);
+// integration boxes of the single-scene kernels (the size of the mark array)
+int integrate_boxes(const Grid& g);
 // every scene's ray cast, persistent over all scenes' tiles; shape 0: 8x4, 1: 16x2,
 // 2: 4x8 pixels per warp tile; tile_counter: two device unsigneds, zero between launches
 int raycast_tiles(int H, int W, int shape);

@@ -135,9 +135,10 @@ __device__ __forceinline__ void integrate_prep_tile(int tile, int lane, const fl
     const int x0 = (tile % ntx) * kBoundTile, y0 = (tile / ntx) * kBoundTile;
     if (tile == 0) {
         // T^-1 for integration, and the pose it inverts (the next frame's ICP reuses
-        // the inverse while the pose is unchanged)
+        // the inverse while the pose is unchanged); an empty mark list
         inv4_warp(st->T, st->Tinv);
         if (lane < 16) st->Tinv_src[lane] = st->T[lane];
+        if (lane == 0) st->mark_count = 0u;
     }
     float lo = INFINITY, hi = -INFINITY;
 #pragma unroll
@@ -183,11 +184,15 @@ __global__ void __launch_bounds__(256) integrate_prep_batch_kernel(const SceneDe
 }
 
 // Integration proceeds in boxes of kIntTx x kIntTy voxel columns by zchunk voxels along
-// z: one block of kIntTx x kIntTy threads per box, one thread per column segment.  A box
-// is culled as a whole, then each voxel.  (A second cull of each thread's segment by the
-// same tests cost more than the voxels it removed: 48.9 -> 44.7 us per c1 frame without
-// it.)
+// z, a block of kIntTx x kIntTy threads per box, one thread per column segment.  A single
+// scene's boxes are chosen from the depth tiles' side (integrate_mark_kernel: the boxes
+// a tile's pixels can update are marked, then listed); a batch of scenes decides each
+// box by its corners and its footprint's depth bounds (box_live).  Within a box every
+// voxel runs the reference's tests.  (A further cull of each thread's segment by the
+// corner tests cost more than the voxels it removed: 48.9 -> 44.7 us per c1 frame
+// without it.)
 constexpr int kIntTx = 32, kIntTy = 8;
+constexpr int kZB = 4;  // voxels of a column segment whose loads are issued together
 
 // The frame's constants of integration beside the pose (which the kernels read from
 // State).
@@ -424,62 +429,91 @@ __device__ __forceinline__ void integrate_at(const Vol& vol, const float2* __res
     const float ulo = 0.5f - 1e-3f, uhi = (float)W + 0.5f + 1e-3f * (float)W;
     const float vlo = 0.5f - 1e-3f, vhi = (float)H + 0.5f + 1e-3f * (float)H;
     const float inv_trunc = 1.f / g.trunc;
-    for (int z = z0; z < z1; ++z, lin += zstride) {
-        if (may_skip && rbase + z >= p.skip_from) continue;
-        const float vcz = centre(z, g.sz, g.vd);
-        // the reference's tests are independent rejections (all must pass), so the
-        // cheapest runs first: the in-front test (:57-73) needs no projection
-        const float tdz = vcz - tz;
-        const float front = f0 + az * tdz;
-        if (!(front > 0)) continue;
-        const float lx = (a0 + ti[2] * vcz) + ti[3];
-        const float ly = (a1 + ti[6] * vcz) + ti[7];
-        const float lz = (a2 + ti[10] * vcz) + ti[11];
-        // K (lx, ly, lz) with K's structural zeros dropped; adding a 0 product changes at
-        // most the sign of a zero result, which projects to pixel 0 and is rejected
-        // either way
-        const float px = fx * lx + cx * lz;
-        const float py = fy * ly + cy * lz;
-        float r;
-        asm("rcp.approx.f32 %0, %1;" : "=f"(r) : "f"(lz));
-        const float qu = px * r, qv = py * r;
-        if (qu < ulo || qu > uhi || qv < vlo || qv > vhi) continue;
-        const int u = (int)roundf(px / lz);
-        const int v = (int)roundf(py / lz);
-        if (u < 1 || u > W || v < 1 || v > H) continue;
-        const float2 e = __ldg(tab + (v - 1) * W + (u - 1));
-        if (isnan(e.x)) continue;
-        float tm;
-        if (Vol::kLean)
-            asm("sqrt.approx.f32 %0, %1;" : "=f"(tm) : "f"(m0 + tdz * tdz));
-        else
-            tm = sqrtf(m0 + tdz * tdz);
-        const float frk = e.x - e.y * tm;
-        const bool ahead = frk > 0 && frk <= g.sdf_max;
-        const bool behind = frk <= 0 && frk >= g.sdf_min;
-        if (!ahead && !behind) continue;
-        const float fq = Vol::kLean ? frk * inv_trunc : frk / g.trunc;
-        const float f = ahead ? fminf(1.f, fq) : fmaxf(-1.f, fq);
+    // The column segment in batches of kZB voxels: a batch first runs every voxel's tests
+    // up to its pixel, then issues the table loads of the voxels that reach one together,
+    // then the volume loads of the voxels that are updated, so that a thread's loads
+    // overlap instead of following one another.  Each voxel is read and written by its
+    // own thread only, so the order changes no value.  (41.9 against 45.6 us per c1 frame
+    // with the listed boxes; the pass is a per-box latency chain.)
+    for (int zb = z0; zb < z1; zb += kZB, lin += kZB * zstride) {
+        int pix[kZB];
+#pragma unroll
+        for (int k = 0; k < kZB; ++k) {
+            const int z = zb + k;
+            pix[k] = -1;
+            if (z >= z1 || (may_skip && rbase + z >= p.skip_from)) continue;
+            const float vcz = centre(z, g.sz, g.vd);
+            const float tdz = vcz - tz;
+            const float front = f0 + az * tdz;
+            if (!(front > 0)) continue;
+            const float lx = (a0 + ti[2] * vcz) + ti[3];
+            const float ly = (a1 + ti[6] * vcz) + ti[7];
+            const float lz = (a2 + ti[10] * vcz) + ti[11];
+            const float px = fx * lx + cx * lz;
+            const float py = fy * ly + cy * lz;
+            float r;
+            asm("rcp.approx.f32 %0, %1;" : "=f"(r) : "f"(lz));
+            const float qu = px * r, qv = py * r;
+            if (qu < ulo || qu > uhi || qv < vlo || qv > vhi) continue;
+            const int u = (int)roundf(px / lz);
+            const int v = (int)roundf(py / lz);
+            if (u < 1 || u > W || v < 1 || v > H) continue;
+            pix[k] = (v - 1) * W + (u - 1);
+        }
+        float2 e[kZB];
+#pragma unroll
+        for (int k = 0; k < kZB; ++k) e[k] = pix[k] >= 0 ? __ldg(tab + pix[k]) : make_float2(qnan(), 0.f);
+        float fv[kZB];
+        bool upd[kZB];
+#pragma unroll
+        for (int k = 0; k < kZB; ++k) {
+            upd[k] = false;
+            fv[k] = 0.f;
+            if (isnan(e[k].x)) continue;
+            const float tdz = centre(zb + k, g.sz, g.vd) - tz;
+            float tm;
+            if (Vol::kLean)
+                asm("sqrt.approx.f32 %0, %1;" : "=f"(tm) : "f"(m0 + tdz * tdz));
+            else
+                tm = sqrtf(m0 + tdz * tdz);
+            const float frk = e[k].x - e[k].y * tm;
+            const bool ahead = frk > 0 && frk <= g.sdf_max;
+            const bool behind = frk <= 0 && frk >= g.sdf_min;
+            if (!ahead && !behind) continue;
+            const float fq = Vol::kLean ? frk * inv_trunc : frk / g.trunc;
+            fv[k] = ahead ? fminf(1.f, fq) : fmaxf(-1.f, fq);
+            upd[k] = true;
+        }
         if (FIRST) {
-            vol.store(lin, f, 1.0f);
+#pragma unroll
+            for (int k = 0; k < kZB; ++k)
+                if (upd[k]) vol.store(lin + k * zstride, fv[k], 1.0f);
         } else {
-            float t, w;
-            vol.load(lin, t, w);
-            if (isnan(t)) t = 0.0f;
-            if (isnan(w)) w = 0.0f;
-            if (Vol::kLean) {
-                float rw;
-                asm("rcp.approx.f32 %0, %1;" : "=f"(rw) : "f"(w + 1.0f));
-                vol.store(lin, fmaf(w, t, f) * rw, w + 1.0f);
-            } else {
-                vol.store(lin, (w * t + 1.0f * f) / (w + 1.0f), w + 1.0f);
+            float t[kZB], w[kZB];
+#pragma unroll
+            for (int k = 0; k < kZB; ++k) {
+                t[k] = w[k] = 0.f;
+                if (upd[k]) vol.load(lin + k * zstride, t[k], w[k]);
+            }
+#pragma unroll
+            for (int k = 0; k < kZB; ++k) {
+                if (!upd[k]) continue;
+                const float tk = isnan(t[k]) ? 0.0f : t[k];
+                const float wk = isnan(w[k]) ? 0.0f : w[k];
+                if (Vol::kLean) {
+                    float rw;
+                    asm("rcp.approx.f32 %0, %1;" : "=f"(rw) : "f"(wk + 1.0f));
+                    vol.store(lin + k * zstride, fmaf(wk, tk, fv[k]) * rw, wk + 1.0f);
+                } else {
+                    vol.store(lin + k * zstride, (wk * tk + 1.0f * fv[k]) / (wk + 1.0f), wk + 1.0f);
+                }
             }
         }
     }
 }
 
-// One block per box.  Warp 0 decides whether the box can hold an updated voxel; a dead
-// box's other warps do nothing but wait for that decision.
+// One block per box (the batched scenes).  Warp 0 decides whether the box can hold an
+// updated voxel; a dead box's other warps do nothing but wait for that decision.
 template <class Vol, bool FIRST>
 __device__ __forceinline__ void integrate_box(const Vol& vol, const float2* __restrict__ tab,
                                               const State* __restrict__ st, const Grid& g, const IntegrateParams& p,
@@ -494,16 +528,169 @@ __device__ __forceinline__ void integrate_box(const Vol& vol, const float2* __re
     if (s_live) integrate_at<Vol, FIRST>(vol, tab, st, g, p, bx, by, bz);
 }
 
+// ---- box marks from the depth tiles (single-scene integration) ----
+//
+// Which boxes can hold an updated voxel is decided from the pixels' side: a voxel is
+// updated only through a pixel (u, v) with a depth D, and then (a) its projection rounds
+// to (u, v), so its centre lies in that pixel's frustum widened by half a pixel and by
+// the projection's rounding error, and (b) its camera depth lz lies in the band of D
+// (band_culled's two tests, each false for it).  For each 8x8 depth tile with (dmin,
+// dmax) of its nonzero depths, every such voxel lies in the tile's frustum between the
+// camera depths z_a and z_b of those tests; the frustum is cut into slabs of kSlab mm,
+// each slab (a convex hexahedron) lies in the box spanned by its eight corners in the
+// world, and every integration box that overlaps that (widened) box is marked (plain
+// stores of 1).  A compaction pass then lists the marked boxes and clears their marks,
+// so every integration starts from unmarked boxes.  Near the camera (lz below kNearZ) the pixel margin grows without
+// bound, so the boxes within kNearR of the camera centre are marked instead.
+constexpr float kSlab = 80.f;     // mm of camera depth per slab
+
+constexpr float kNearZ = 100.f;   // slabs start at this camera depth
+constexpr float kNearR = 250.f;   // mm around the camera centre marked unconditionally
+
+__device__ __forceinline__ void mark_world_box(float3 lo, float3 hi, const Grid& g, unsigned* __restrict__ mark,
+                                               int zchunk, int nbx, int nby, int nbz)
+{
+    // the grid's extent with a voxel to spare (the conversions below stay in range); NaN
+    // corners (a NaN pose, which updates nothing) leave lo > hi
+    const float gx0 = ((float)g.sx - 1.f) * g.vd, gx1 = ((float)(g.sx + g.dx) + 1.f) * g.vd;
+    const float gy0 = ((float)g.sy - 1.f) * g.vd, gy1 = ((float)(g.sy + g.dy) + 1.f) * g.vd;
+    const float gz0 = ((float)g.sz - 1.f) * g.vd, gz1 = ((float)(g.sz + g.dz) + 1.f) * g.vd;
+    if (!(lo.x <= gx1 && hi.x >= gx0 && lo.y <= gy1 && hi.y >= gy0 && lo.z <= gz1 && hi.z >= gz0)) return;
+    lo = make_float3(fmaxf(lo.x, gx0), fmaxf(lo.y, gy0), fmaxf(lo.z, gz0));
+    hi = make_float3(fminf(hi.x, gx1), fminf(hi.y, gy1), fminf(hi.z, gz1));
+    // voxel i's centre along x is (i + sx) vd + vd / 2; one voxel more on each side
+    const float ivd = 1.f / g.vd;
+    const int i0 = max(0, (int)floorf((lo.x - 0.5f * g.vd) * ivd) - g.sx - 1);
+    const int i1 = min(g.dx - 1, (int)ceilf((hi.x - 0.5f * g.vd) * ivd) - g.sx + 1);
+    const int j0 = max(0, (int)floorf((lo.y - 0.5f * g.vd) * ivd) - g.sy - 1);
+    const int j1 = min(g.dy - 1, (int)ceilf((hi.y - 0.5f * g.vd) * ivd) - g.sy + 1);
+    const int k0 = max(0, (int)floorf((lo.z - 0.5f * g.vd) * ivd) - g.sz - 1);
+    const int k1 = min(g.dz - 1, (int)ceilf((hi.z - 0.5f * g.vd) * ivd) - g.sz + 1);
+    if (i0 > i1 || j0 > j1 || k0 > k1) return;
+    for (int bz = k0 / zchunk; bz <= k1 / zchunk; ++bz)
+        for (int by = j0 / kIntTy; by <= j1 / kIntTy; ++by)
+            for (int bx = i0 / kIntTx; bx <= i1 / kIntTx; ++bx) mark[(bz * nby + by) * nbx + bx] = 1u;
+}
+
+// one warp per depth tile, the tile's slabs over its lanes; block 0's first warp also
+// marks the boxes around the camera
+__global__ void __launch_bounds__(256) integrate_mark_kernel(const float2* __restrict__ tab,
+                                                             const State* __restrict__ st, Grid g, IntegrateParams p,
+                                                             unsigned* __restrict__ mark, int nbx, int nby, int nbz)
+{
+    wait_for_producer();
+    // the compaction may be scheduled now; it waits for this kernel before reading marks
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    const int lane = threadIdx.x & 31;
+    const int tile = blockIdx.x * 8 + (threadIdx.x >> 5);
+    const int ntx = bound_tiles_x(p.W), tiles = ntx * ((p.H + kBoundTile - 1) / kBoundTile);
+    float T[12];
+#pragma unroll
+    for (int k = 0; k < 12; ++k) T[k] = st->T[k];
+    const float tmax = fmaxf(fmaxf(fabsf(T[3]), fabsf(T[7])), fabsf(T[11]));
+    if (tile == 0 && lane == 0) {
+        const float r = kNearR + 2.f * g.vd;
+        mark_world_box(make_float3(T[3] - r, T[7] - r, T[11] - r), make_float3(T[3] + r, T[7] + r, T[11] + r), g,
+                       mark, p.zchunk, nbx, nby, nbz);
+    }
+    if (tile >= tiles) return;
+    const float2 b = tab[p.H * p.W + tile];
+    const float dmin = b.x, dmax = b.y;
+    if (!(dmin <= dmax)) return;  // no pixel with depth in this tile
+    // band_culled's margins: a voxel updated through a pixel with depth D in [dmin, dmax]
+    // has z_a <= lz <= z_b; widened by 1 % and 2 mm for the evaluation of these bounds
+    const float eps_t = 0x1p-18f * (tmax + 4.f * p.lam_max + 1.f);
+    const float abs_t = 0x1p-19f * tmax + 1.f;
+    const float hi_band = fmaxf(g.sdf_max, 0.f), lo_band = fminf(g.sdf_min, 0.f);
+    const float z_a = (dmin * (1.f - eps_t) - hi_band - 2.f * abs_t) / ((1.f + p.depth_eps) * (1.f + eps_t)) * 0.99f - 2.f;
+    const float z_b = (dmax * (1.f + eps_t) - lo_band + 2.f * abs_t) / ((1.f - p.depth_eps) * (1.f - eps_t)) * 1.01f + 2.f;
+    const float z_lo = fmaxf(z_a, kNearZ);
+    if (!(z_b > z_lo)) return;
+    const int nslab = (int)ceilf((z_b - z_lo) / kSlab);
+    // rounding error of a voxel's camera coordinates (integrate_at's evaluation): at
+    // most 2^-19 of a generous bound on their terms' magnitudes, the grid's extent plus
+    // the camera's distance from the origin; the pixel margin is taken at the nearest
+    // slab depth z_lo, where it is largest: one pixel for the rounding to a pixel centre
+    // plus the projection's error
+    const float ext = (float)(max(max(abs(g.sx), abs(g.sx + g.dx)), max(max(abs(g.sy), abs(g.sy + g.dy)),
+                                                                      max(abs(g.sz), abs(g.sz + g.dz))))) *
+                      g.vd;
+    const float err_l = 0x1p-19f * 4.f * (ext + tmax);
+    const float mpx = 1.f + (fmaxf(p.fx, p.fy) + fmaxf(fabsf(p.cx), fabsf(p.cy)) + (float)max(p.W, p.H) + 10.f) *
+                                err_l / z_lo + 1e-3f;
+    // the tile's pixels (1-based) span [x0 + 0.5, x0 + 8.5] in projected coordinates; the
+    // four corner rays (camera x / z, y / z) of that range widened by mpx, in the world
+    const float u_a = (float)((tile % ntx) * kBoundTile) + 0.5f, v_a = (float)((tile / ntx) * kBoundTile) + 0.5f;
+    const float rx0 = (u_a - mpx - p.cx) / p.fx, rx1 = (u_a + 8.f + mpx - p.cx) / p.fx;
+    const float ry0 = (v_a - mpx - p.cy) / p.fy, ry1 = (v_a + 8.f + mpx - p.cy) / p.fy;
+    float3 wr[4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        const float X = (c & 1) ? rx1 : rx0, Y = (c & 2) ? ry1 : ry0;
+        wr[c] = make_float3(T[0] * X + T[1] * Y + T[2], T[4] * X + T[5] * Y + T[6], T[8] * X + T[9] * Y + T[10]);
+    }
+    const float rmax = fmaxf(fmaxf(fabsf(rx0), fabsf(rx1)), fmaxf(fabsf(ry0), fabsf(ry1)));
+    for (int k = lane; k < nslab; k += 32) {
+        const float za = z_lo + (float)k * kSlab, zb = fminf(z_lo + (float)(k + 1) * kSlab, z_b);
+        // the slab's corners t + z R (x/z, y/z, 1) for z = za, zb; each coordinate is
+        // within a relative 2^-20 of its terms' magnitudes, covered by e (and a millimetre)
+        float3 lo = make_float3(INFINITY, INFINITY, INFINITY), hi = make_float3(-INFINITY, -INFINITY, -INFINITY);
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+            const float z = (c & 4) ? zb : za;
+            const float3 w = wr[c & 3];
+            const float wx = w.x * z + T[3], wy = w.y * z + T[7], wz = w.z * z + T[11];
+            lo = make_float3(fminf(lo.x, wx), fminf(lo.y, wy), fminf(lo.z, wz));
+            hi = make_float3(fmaxf(hi.x, wx), fmaxf(hi.y, wy), fmaxf(hi.z, wz));
+        }
+        const float e = 0x1p-17f * ((2.f * rmax + 1.f) * 2.f * zb + tmax) + 1.f;
+        lo = make_float3(lo.x - e, lo.y - e, lo.z - e);
+        hi = make_float3(hi.x + e, hi.y + e, hi.z + e);
+        mark_world_box(lo, hi, g, mark, p.zchunk, nbx, nby, nbz);
+    }
+}
+
+// The marked boxes in order, as a list after the marks (mark + nboxes), and the marks
+// cleared: one thread per box, one atomic per warp for the warp's marked boxes.
+__global__ void __launch_bounds__(256) integrate_list_kernel(State* st, unsigned* __restrict__ mark, int nboxes)
+{
+    wait_for_producer();
+    // integration may be scheduled now; it waits for this kernel before reading the list
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    const bool m = b < nboxes && mark[b] != 0u;
+    const unsigned ball = __ballot_sync(0xffffffffu, m);
+    if (!ball) return;
+    unsigned base = 0u;
+    if (lane == 0) base = atomicAdd(&st->mark_count, (unsigned)__popc(ball));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (m) {
+        mark[nboxes + base + __popc(ball & ((1u << lane) - 1u))] = (unsigned)b;
+        mark[b] = 0u;
+    }
+}
+
+// Persistent: the blocks take the boxes on the mark list in strides of the grid (the
+// list is in marking order, which spreads neighbouring boxes over the blocks); a block
+// of 32 x 8 threads updates one box at a time, a thread its 16-voxel column segment.
 template <class Vol, bool FIRST>
 __global__ void __launch_bounds__(kIntTx* kIntTy, 5) integrate_kernel(Vol vol, const float2* __restrict__ tab,
                                                                    const State* __restrict__ st, Grid g,
-                                                                   IntegrateParams p)
+                                                                   IntegrateParams p,
+                                                                   const unsigned* __restrict__ mark, int nbx, int nby,
+                                                                   int nboxes)
 {
     wait_for_producer();
-    // the ray cast may be scheduled once every box has started; it waits for this kernel
-    // before reading the volume
+    // the ray cast may be scheduled once every block has started; it waits for this
+    // kernel before reading the volume
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-    integrate_box<Vol, FIRST>(vol, tab, st, g, p, blockIdx.x, blockIdx.y, blockIdx.z);
+    const unsigned n = st->mark_count;
+    const unsigned* list = mark + nboxes;
+    for (unsigned i = blockIdx.x; i < n; i += gridDim.x) {
+        const int box = (int)list[i];
+        integrate_at<Vol, FIRST>(vol, tab, st, g, p, box % nbx, (box / nbx) % nby, box / (nbx * nby));
+    }
 }
 
 __device__ __forceinline__ VolF32 scene_volume(const SceneDev& d, VolF32*) { return VolF32{d.tsdf, d.weight}; }
@@ -1004,6 +1191,22 @@ int raycast_blocks()
     return blocks[dev];
 }
 
+// once per device, outside any stream capture: sizes the persistent integration grid
+int integrate_blocks()
+{
+    static int blocks[64] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64) return 152 * 5;
+    if (!blocks[dev]) {
+        int sms = 0, per_sm = 0;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, integrate_kernel<VolF16, false>, kIntTx * kIntTy, 0);
+        blocks[dev] = (sms > 0 ? sms : 152) * (per_sm > 0 ? per_sm : 5);
+    }
+    return blocks[dev];
+}
+
 void launch_integrate_prep(const float* depth, float2* tab, const Camera& cam, State* st, cudaStream_t s)
 {
     launch_pdl(integrate_prep_kernel, dim3((depth_bound_tiles(cam.H, cam.W) + 7) / 8), dim3(256), 0, s, depth, tab,
@@ -1054,28 +1257,36 @@ IntegrateParams host_params(const Camera& cam, int zchunk, long long skip_from)
 
 template <class Vol>
 void integrate_launch(Vol vol, const float2* tab, const State* st, const Grid& g, const Camera& cam,
-                      long long skip_from, bool first, cudaStream_t s)
+                      long long skip_from, bool first, unsigned* mark, cudaStream_t s)
 {
     const IntegrateParams p = host_params(cam, kZChunk, skip_from);
     const dim3 block(kIntTx, kIntTy);
     const dim3 grid((g.dx + kIntTx - 1) / kIntTx, (g.dy + kIntTy - 1) / kIntTy, (g.dz + kZChunk - 1) / kZChunk);
+    const int nboxes = (int)(grid.x * grid.y * grid.z);
+    launch_pdl(integrate_mark_kernel, dim3((depth_bound_tiles(cam.H, cam.W) + 7) / 8), dim3(256), 0, s, tab, st, g, p,
+               mark, (int)grid.x, (int)grid.y, (int)grid.z);
+    launch_pdl(integrate_list_kernel, dim3((nboxes + 255) / 256), dim3(256), 0, s, const_cast<State*>(st), mark,
+               nboxes);
+    const dim3 blocks(integrate_blocks());
     if (first)
-        launch_pdl(integrate_kernel<Vol, true>, grid, block, 0, s, vol, tab, st, g, p);
+        launch_pdl(integrate_kernel<Vol, true>, blocks, block, 0, s, vol, tab, st, g, p, (const unsigned*)mark,
+                   (int)grid.x, (int)grid.y, nboxes);
     else
-        launch_pdl(integrate_kernel<Vol, false>, grid, block, 0, s, vol, tab, st, g, p);
+        launch_pdl(integrate_kernel<Vol, false>, blocks, block, 0, s, vol, tab, st, g, p, (const unsigned*)mark,
+                   (int)grid.x, (int)grid.y, nboxes);
 }
 }  // namespace
 
 void launch_integrate_f32(float* tsdf, float* weight, const float2* tab, const State* st, const Grid& g,
-                          const Camera& cam, long long skip_from, bool first, cudaStream_t s)
+                          const Camera& cam, long long skip_from, bool first, unsigned* mark, cudaStream_t s)
 {
-    integrate_launch(VolF32{tsdf, weight}, tab, st, g, cam, skip_from, first, s);
+    integrate_launch(VolF32{tsdf, weight}, tab, st, g, cam, skip_from, first, mark, s);
 }
 
 void launch_integrate_f16(__half2* vol, const float2* tab, const State* st, const Grid& g, const Camera& cam,
-                          long long skip_from, bool first, cudaStream_t s)
+                          long long skip_from, bool first, unsigned* mark, cudaStream_t s)
 {
-    integrate_launch(VolF16{vol}, tab, st, g, cam, skip_from, first, s);
+    integrate_launch(VolF16{vol}, tab, st, g, cam, skip_from, first, mark, s);
 }
 
 void launch_raycast_f32(const float* tsdf, const float* depth, float4* pv, float4* pn, int32_t* hit,
@@ -1131,6 +1342,8 @@ void launch_integrate_batch_persistent(const SceneDev* scenes, int n_scenes, int
                        total_boxes, counter);
     }
 }
+
+int integrate_boxes(const Grid& g) { return integrate_tiles(g, kZChunk); }
 
 int integrate_tiles(const Grid& g, int zchunk)
 {

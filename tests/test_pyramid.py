@@ -53,7 +53,7 @@ def test_pyramid_pipeline_bit_exact_with_oracle(oracle, small_seq):
         h.incoming_frame(depths[k])
         p.incoming(depths[k])
         assert np.array_equal(h.pose().view(np.uint32), p.pose.view(np.uint32)), f"frame {k}"
-    assert h.kernels_per_frame() == 1 + 3 * 2 + 2 * 19 + 3
+    assert h.kernels_per_frame() == 1 + 3 * 2 + 2 * 19 + 5
     nc, _ = h.icp_stats()
     assert len(nc) == 19 and nc[-1] > 100
     t, w = h.volume()
@@ -89,6 +89,6 @@ def test_precision_form_pyramid_tracks_like_the_plain_pyramid(oracle, small_seq)
         eg = np.linalg.norm(h.pose().astype(np.float64)[:3, 3] - gt[:3, 3])
         eo = np.linalg.norm(p.pose.astype(np.float64)[:3, 3] - gt[:3, 3])
         assert eg <= eo + 1.0 + 0.5 * eo, (k, eg, eo)
-    assert h.kernels_per_frame() == 1 + 3 * 2 + 19 + 3
+    assert h.kernels_per_frame() == 1 + 3 * 2 + 19 + 5
     nc, _ = h.icp_stats()
     assert len(nc) == 19 and min(nc) > 10
