@@ -543,12 +543,13 @@ __device__ __forceinline__ void integrate_box(const Vol& vol, const float2* __re
 // so every integration starts from unmarked boxes.  Near the camera (lz below kNearZ) the pixel margin grows without
 // bound, so the boxes within kNearR of the camera centre are marked instead.
 constexpr float kSlab = 80.f;     // mm of camera depth per slab
+constexpr int kMarkLanes = 8;     // lanes per depth tile (slabs over them)
 
 constexpr float kNearZ = 100.f;   // slabs start at this camera depth
 constexpr float kNearR = 250.f;   // mm around the camera centre marked unconditionally
 
 __device__ __forceinline__ void mark_world_box(float3 lo, float3 hi, const Grid& g, unsigned* __restrict__ mark,
-                                               int zchunk, int nbx, int nby, int nbz)
+                                               int zchunk, int nbx, int nby, int nbz, int first = 0, int step = 1)
 {
     // the grid's extent with a voxel to spare (the conversions below stay in range); NaN
     // corners (a NaN pose, which updates nothing) leave lo > hi
@@ -567,13 +568,15 @@ __device__ __forceinline__ void mark_world_box(float3 lo, float3 hi, const Grid&
     const int k0 = max(0, (int)floorf((lo.z - 0.5f * g.vd) * ivd) - g.sz - 1);
     const int k1 = min(g.dz - 1, (int)ceilf((hi.z - 0.5f * g.vd) * ivd) - g.sz + 1);
     if (i0 > i1 || j0 > j1 || k0 > k1) return;
-    for (int bz = k0 / zchunk; bz <= k1 / zchunk; ++bz)
-        for (int by = j0 / kIntTy; by <= j1 / kIntTy; ++by)
-            for (int bx = i0 / kIntTx; bx <= i1 / kIntTx; ++bx) mark[(bz * nby + by) * nbx + bx] = 1u;
+    // the boxes of the range, from `first` in steps of `step` (the callers' lanes)
+    const int x0 = i0 / kIntTx, y0 = j0 / kIntTy, z0 = k0 / zchunk;
+    const int nx = i1 / kIntTx - x0 + 1, ny = j1 / kIntTy - y0 + 1, nz = k1 / zchunk - z0 + 1;
+    for (int f = first; f < nx * ny * nz; f += step)
+        mark[((z0 + f / (nx * ny)) * nby + y0 + (f / nx) % ny) * nbx + x0 + f % nx] = 1u;
 }
 
-// one warp per depth tile, the tile's slabs over its lanes; block 0's first warp also
-// marks the boxes around the camera
+// kMarkLanes threads per depth tile, the tile's slabs over them; block 0's first warp
+// also marks the boxes around the camera
 __global__ void __launch_bounds__(256) integrate_mark_kernel(const float2* __restrict__ tab,
                                                              const State* __restrict__ st, Grid g, IntegrateParams p,
                                                              unsigned* __restrict__ mark, int nbx, int nby, int nbz)
@@ -581,17 +584,17 @@ __global__ void __launch_bounds__(256) integrate_mark_kernel(const float2* __res
     wait_for_producer();
     // the compaction may be scheduled now; it waits for this kernel before reading marks
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-    const int lane = threadIdx.x & 31;
-    const int tile = blockIdx.x * 8 + (threadIdx.x >> 5);
+    const int lane = threadIdx.x % kMarkLanes;
+    const int tile = blockIdx.x * (256 / kMarkLanes) + threadIdx.x / kMarkLanes;
     const int ntx = bound_tiles_x(p.W), tiles = ntx * ((p.H + kBoundTile - 1) / kBoundTile);
     float T[12];
 #pragma unroll
     for (int k = 0; k < 12; ++k) T[k] = st->T[k];
     const float tmax = fmaxf(fmaxf(fabsf(T[3]), fabsf(T[7])), fabsf(T[11]));
-    if (tile == 0 && lane == 0) {
+    if (blockIdx.x == 0 && threadIdx.x < 32) {
         const float r = kNearR + 2.f * g.vd;
         mark_world_box(make_float3(T[3] - r, T[7] - r, T[11] - r), make_float3(T[3] + r, T[7] + r, T[11] + r), g,
-                       mark, p.zchunk, nbx, nby, nbz);
+                       mark, p.zchunk, nbx, nby, nbz, threadIdx.x, 32);
     }
     if (tile >= tiles) return;
     const float2 b = tab[p.H * p.W + tile];
@@ -630,7 +633,7 @@ __global__ void __launch_bounds__(256) integrate_mark_kernel(const float2* __res
         wr[c] = make_float3(T[0] * X + T[1] * Y + T[2], T[4] * X + T[5] * Y + T[6], T[8] * X + T[9] * Y + T[10]);
     }
     const float rmax = fmaxf(fmaxf(fabsf(rx0), fabsf(rx1)), fmaxf(fabsf(ry0), fabsf(ry1)));
-    for (int k = lane; k < nslab; k += 32) {
+    for (int k = lane; k < nslab; k += kMarkLanes) {
         const float za = z_lo + (float)k * kSlab, zb = fminf(z_lo + (float)(k + 1) * kSlab, z_b);
         // the slab's corners t + z R (x/z, y/z, 1) for z = za, zb; each coordinate is
         // within a relative 2^-20 of its terms' magnitudes, covered by e (and a millimetre)
@@ -1263,7 +1266,8 @@ void integrate_launch(Vol vol, const float2* tab, const State* st, const Grid& g
     const dim3 block(kIntTx, kIntTy);
     const dim3 grid((g.dx + kIntTx - 1) / kIntTx, (g.dy + kIntTy - 1) / kIntTy, (g.dz + kZChunk - 1) / kZChunk);
     const int nboxes = (int)(grid.x * grid.y * grid.z);
-    launch_pdl(integrate_mark_kernel, dim3((depth_bound_tiles(cam.H, cam.W) + 7) / 8), dim3(256), 0, s, tab, st, g, p,
+    launch_pdl(integrate_mark_kernel, dim3((depth_bound_tiles(cam.H, cam.W) * kMarkLanes + 255) / 256), dim3(256), 0, s,
+               tab, st, g, p,
                mark, (int)grid.x, (int)grid.y, (int)grid.z);
     launch_pdl(integrate_list_kernel, dim3((nboxes + 255) / 256), dim3(256), 0, s, const_cast<State*>(st), mark,
                nboxes);
