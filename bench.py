@@ -432,11 +432,27 @@ def run_form(args, dist, form, cfg, frames, order, fresh, stream, **extra):
         e2e = {"value": args.steps * dist.world / dt, "unit": "frames/s", "h2d_bytes_per_step": fbytes,
                "d2h_bytes_per_step": 64}
 
+    # integration's live voxels: those whose weight one incoming frame changes, counted
+    # from the volume read back before and after it (outside every timed region)
+    k = n_total + args.profile_frames + (0 if args.no_e2e else args.steps)
+    while k < len(order) and fresh[k]:
+        k += 1
+    live = None
+    if k < len(order) and getattr(args, "live_count", True):
+        h.synchronize()
+        _, w0 = h.volume()
+        h.incoming_frame_device(dptr(k))
+        h.synchronize()
+        _, w1 = h.volume()
+        live = int(np.count_nonzero(np.nan_to_num(w1, nan=-1.0) != np.nan_to_num(w0, nan=-1.0)))
+        del w0, w1
+
     ate = trajectory_error(h, dev, fbytes, len(frames), cfg.name) if not args.no_ate else None
     sync = synced_error(h, dev, fbytes, cfg.name) if not args.no_ate else None
     h.close()
     return {"value": args.steps * dist.world / (ms_max / 1000.0), "ms_per_step": ms_max / args.steps,
             "e2e": e2e, "stages_ms": stage_ms, "gpu_launches": launches, "clocks": clk, "ate": ate,
+            "live_voxels": live,
             "synced_fp64": sync, "tsdf": FORMS[form]["tsdf"]}
 
 
@@ -458,12 +474,12 @@ def roofline_of(cfg, r, form: str):
         "icp": 49 * cam.height * cam.width * 10,
         "raycast": 45 * (4 if tsdf == "f32" else 2) * int(0.83 * cam.height * cam.width),
     }
-    kernels = {"integration": "integrate_prep_kernel + integrate_kernel",
+    kernels = {"integration": "integrate_prep_kernel + integrate_mark_kernel + integrate_list_kernel + integrate_kernel",
                "icp": "10 x (icp_group_kernel + icp_solve_kernel)" if form == "plain" else "10 x icp_precise_kernel",
                "raycast": "raycast_kernel"}
     keys = {"integration": f"integration_{tsdf}", "icp": f"icp_{form}", "raycast": f"raycast_{tsdf}"}
     # what limits each stage (ncu evidence in profiles/): none of them is HBM-bound
-    limiter = {"integration": "latency: one warp decides each 32x8x16 box while the block waits",
+    limiter = {"integration": "latency: the update's per-box chain over the boxes marked from the depth tiles' frusta",
                "icp": "latency: a serial chain of 10 association / reduction / solve passes, L2-resident",
                "raycast": "instruction issue (ALU pipe), L2-resident gathers"}
     stages = {}
@@ -480,6 +496,13 @@ def roofline_of(cfg, r, form: str):
     ig["achieved"] = (ig["traffic"] / (st["integration"] / 1000.0) / 1e9
                       if ig["traffic"] and st["integration"] > 0 else None)
     ig["frac"] = ig["achieved"] / peak if ig["achieved"] else None
+    # and the bytes of the voxels it actually updates (read and written, value + weight),
+    # counted at run time
+    if r.get("live_voxels"):
+        ig["live_voxels"] = r["live_voxels"]
+        ig["live_bytes"] = r["live_voxels"] * (16 if tsdf == "f32" else 8)
+        ig["live_gbs"] = ig["live_bytes"] / (st["integration"] / 1000.0) / 1e9 if st["integration"] > 0 else None
+        ig["live_frac"] = ig["live_gbs"] / peak if ig["live_gbs"] else None
     dom = max(stages, key=lambda s: stages[s]["ms"])
     return {"bound": "hbm", "achieved": stages[dom]["achieved"], "peak": peak, "unit": "GB/s",
             "frac": stages[dom]["frac"], "traffic": stages[dom]["traffic"], "kernel": kernels[dom],
@@ -712,8 +735,8 @@ def run_precision_c2(args, dist, stream) -> dict:
 
     cfg = scene.config("c2")
     sub = argparse.Namespace(**vars(args))
-    sub.steps, sub.warmup, sub.profile_frames, sub.no_e2e = 100, 3, 5, True
-    n_all = 1 + sub.warmup + sub.steps + sub.profile_frames
+    sub.steps, sub.warmup, sub.profile_frames, sub.no_e2e, sub.live_count = 100, 3, 5, True, False
+    n_all = 1 + sub.warmup + sub.steps + sub.profile_frames + 4
     seq = scene.sequence(cfg, frames=UNIQUE_FRAMES)
     frames = seq.depths(UNIQUE_FRAMES)
     order = pingpong(UNIQUE_FRAMES, n_all)
@@ -736,8 +759,8 @@ def run_pyramid_c1(args, dist, stream) -> dict:
 
     cfg = scene.config("c1")
     sub = argparse.Namespace(**vars(args))
-    sub.steps, sub.warmup, sub.profile_frames, sub.no_e2e, sub.no_ate = 100, 3, 5, True, True
-    n_all = 1 + sub.warmup + sub.steps + sub.profile_frames
+    sub.steps, sub.warmup, sub.profile_frames, sub.no_e2e, sub.no_ate, sub.live_count = 100, 3, 5, True, True, False
+    n_all = 1 + sub.warmup + sub.steps + sub.profile_frames + 4
     seq = scene.sequence(cfg, frames=UNIQUE_FRAMES)
     frames = seq.depths(UNIQUE_FRAMES)
     order = pingpong(UNIQUE_FRAMES, n_all)
@@ -759,7 +782,8 @@ def run_gb300(args, dist: Dist):
     n_total = 1 + args.warmup + args.steps
     seq = scene.sequence(cfg, frames=UNIQUE_FRAMES)
     frames = seq.depths(UNIQUE_FRAMES)
-    n_all = n_total + args.profile_frames + (0 if args.no_e2e else args.steps)
+    # and a few frames more for the live-voxel count (run_form)
+    n_all = n_total + args.profile_frames + (0 if args.no_e2e else args.steps) + 4
     order = pingpong(UNIQUE_FRAMES, n_all)
     fresh = restarts(UNIQUE_FRAMES, n_all)
     # a dedicated stream: torch's default stream is the legacy NULL stream (handle 0)
