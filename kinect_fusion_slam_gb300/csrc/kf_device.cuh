@@ -53,6 +53,7 @@ struct State {
     float axis[3];        // "in front of the camera" direction (projective_tsdf.cu:57-71)
     float c_flip;         // ray-cast normal flip threshold (voxel_traversal.cu:361-369)
     unsigned mark_count;  // boxes on integration's mark list (reset by integrate_prep)
+    unsigned mark_near;   // some tile's depth band reaches near the camera (reset likewise)
     double Td[16];        // FP64 pose (precise solve mode)
     unsigned ticket;      // last-block election counter of the ICP reduction
     int iter;             // ICP iterations done in the current frame

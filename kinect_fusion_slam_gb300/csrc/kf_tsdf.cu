@@ -138,7 +138,10 @@ __device__ __forceinline__ void integrate_prep_tile(int tile, int lane, const fl
         // the inverse while the pose is unchanged); an empty mark list
         inv4_warp(st->T, st->Tinv);
         if (lane < 16) st->Tinv_src[lane] = st->T[lane];
-        if (lane == 0) st->mark_count = 0u;
+        if (lane == 0) {
+            st->mark_count = 0u;
+            st->mark_near = 0u;
+        }
     }
     float lo = INFINITY, hi = -INFINITY;
 #pragma unroll
@@ -540,8 +543,10 @@ __device__ __forceinline__ void integrate_box(const Vol& vol, const float2* __re
 // each slab (a convex hexahedron) lies in the box spanned by its eight corners in the
 // world, and every integration box that overlaps that (widened) box is marked (plain
 // stores of 1).  A compaction pass then lists the marked boxes and clears their marks,
-// so every integration starts from unmarked boxes.  Near the camera (lz below kNearZ) the pixel margin grows without
-// bound, so the boxes within kNearR of the camera centre are marked instead.
+// so every integration starts from unmarked boxes.  Near the camera (lz below kNearZ)
+// the pixel margin grows without bound, so when some tile's band reaches below kNearZ
+// the boxes within kNearR of the camera centre are listed too (the compaction tests
+// each box against the camera).
 constexpr float kSlab = 80.f;     // mm of camera depth per slab
 constexpr int kMarkLanes = 8;     // lanes per depth tile (slabs over them)
 
@@ -577,9 +582,9 @@ __device__ __forceinline__ void mark_world_box(float3 lo, float3 hi, const Grid&
 
 // kMarkLanes threads per depth tile, the tile's slabs over them; block 0's first warp
 // also marks the boxes around the camera
-__global__ void __launch_bounds__(256) integrate_mark_kernel(const float2* __restrict__ tab,
-                                                             const State* __restrict__ st, Grid g, IntegrateParams p,
-                                                             unsigned* __restrict__ mark, int nbx, int nby, int nbz)
+__global__ void __launch_bounds__(256) integrate_mark_kernel(const float2* __restrict__ tab, State* st, Grid g,
+                                                             IntegrateParams p, unsigned* __restrict__ mark, int nbx,
+                                                             int nby, int nbz)
 {
     wait_for_producer();
     // the compaction may be scheduled now; it waits for this kernel before reading marks
@@ -591,11 +596,6 @@ __global__ void __launch_bounds__(256) integrate_mark_kernel(const float2* __res
 #pragma unroll
     for (int k = 0; k < 12; ++k) T[k] = st->T[k];
     const float tmax = fmaxf(fmaxf(fabsf(T[3]), fabsf(T[7])), fabsf(T[11]));
-    if (blockIdx.x == 0 && threadIdx.x < 32) {
-        const float r = kNearR + 2.f * g.vd;
-        mark_world_box(make_float3(T[3] - r, T[7] - r, T[11] - r), make_float3(T[3] + r, T[7] + r, T[11] + r), g,
-                       mark, p.zchunk, nbx, nby, nbz, threadIdx.x, 32);
-    }
     if (tile >= tiles) return;
     const float2 b = tab[p.H * p.W + tile];
     const float dmin = b.x, dmax = b.y;
@@ -607,6 +607,7 @@ __global__ void __launch_bounds__(256) integrate_mark_kernel(const float2* __res
     const float hi_band = fmaxf(g.sdf_max, 0.f), lo_band = fminf(g.sdf_min, 0.f);
     const float z_a = (dmin * (1.f - eps_t) - hi_band - 2.f * abs_t) / ((1.f + p.depth_eps) * (1.f + eps_t)) * 0.99f - 2.f;
     const float z_b = (dmax * (1.f + eps_t) - lo_band + 2.f * abs_t) / ((1.f - p.depth_eps) * (1.f - eps_t)) * 1.01f + 2.f;
+    if (z_a < kNearZ && lane == 0) st->mark_near = 1u;  // the boxes around the camera too
     const float z_lo = fmaxf(z_a, kNearZ);
     if (!(z_b > z_lo)) return;
     const int nslab = (int)ceilf((z_b - z_lo) / kSlab);
@@ -655,14 +656,27 @@ __global__ void __launch_bounds__(256) integrate_mark_kernel(const float2* __res
 
 // The marked boxes in order, as a list after the marks (mark + nboxes), and the marks
 // cleared: one thread per box, one atomic per warp for the warp's marked boxes.
-__global__ void __launch_bounds__(256) integrate_list_kernel(State* st, unsigned* __restrict__ mark, int nboxes)
+__global__ void __launch_bounds__(256) integrate_list_kernel(State* st, unsigned* __restrict__ mark, Grid g,
+                                                             int zchunk, int nbx, int nby, int nboxes)
 {
     wait_for_producer();
     // integration may be scheduled now; it waits for this kernel before reading the list
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     const int b = blockIdx.x * blockDim.x + threadIdx.x;
     const int lane = threadIdx.x & 31;
-    const bool m = b < nboxes && mark[b] != 0u;
+    bool m = b < nboxes && mark[b] != 0u;
+    if (!m && b < nboxes && st->mark_near) {
+        // the box's voxel centres against the camera centre widened by kNearR (and two
+        // voxels for the rounding of both)
+        const int bx = b % nbx, by = (b / nbx) % nby, bz = b / (nbx * nby);
+        const float r = kNearR + 2.f * g.vd;
+        const auto overlaps = [&](int i0, int n, int s0, float c) {
+            const float lo = ((float)(i0 + s0) + 0.5f) * g.vd, hi = ((float)(i0 + n - 1 + s0) + 0.5f) * g.vd;
+            return hi >= c - r && lo <= c + r;
+        };
+        m = overlaps(bx * kIntTx, kIntTx, g.sx, st->T[3]) && overlaps(by * kIntTy, kIntTy, g.sy, st->T[7]) &&
+            overlaps(bz * zchunk, zchunk, g.sz, st->T[11]);
+    }
     const unsigned ball = __ballot_sync(0xffffffffu, m);
     if (!ball) return;
     unsigned base = 0u;
@@ -1267,10 +1281,10 @@ void integrate_launch(Vol vol, const float2* tab, const State* st, const Grid& g
     const dim3 grid((g.dx + kIntTx - 1) / kIntTx, (g.dy + kIntTy - 1) / kIntTy, (g.dz + kZChunk - 1) / kZChunk);
     const int nboxes = (int)(grid.x * grid.y * grid.z);
     launch_pdl(integrate_mark_kernel, dim3((depth_bound_tiles(cam.H, cam.W) * kMarkLanes + 255) / 256), dim3(256), 0, s,
-               tab, st, g, p,
+               tab, const_cast<State*>(st), g, p,
                mark, (int)grid.x, (int)grid.y, (int)grid.z);
-    launch_pdl(integrate_list_kernel, dim3((nboxes + 255) / 256), dim3(256), 0, s, const_cast<State*>(st), mark,
-               nboxes);
+    launch_pdl(integrate_list_kernel, dim3((nboxes + 255) / 256), dim3(256), 0, s, const_cast<State*>(st), mark, g,
+               p.zchunk, (int)grid.x, (int)grid.y, nboxes);
     const dim3 blocks(integrate_blocks());
     if (first)
         launch_pdl(integrate_kernel<Vol, true>, blocks, block, 0, s, vol, tab, st, g, p, (const unsigned*)mark,
