@@ -564,14 +564,16 @@ __device__ __forceinline__ void mark_world_box(float3 lo, float3 hi, const Grid&
     if (!(lo.x <= gx1 && hi.x >= gx0 && lo.y <= gy1 && hi.y >= gy0 && lo.z <= gz1 && hi.z >= gz0)) return;
     lo = make_float3(fmaxf(lo.x, gx0), fmaxf(lo.y, gy0), fmaxf(lo.z, gz0));
     hi = make_float3(fminf(hi.x, gx1), fminf(hi.y, gy1), fminf(hi.z, gz1));
-    // voxel i's centre along x is (i + sx) vd + vd / 2; one voxel more on each side
+    // voxel i's centre along x is (i + sx) vd + vd / 2: the voxels with centres in
+    // [lo, hi] (the floor and ceiling are already outward; lo and hi carry the corners'
+    // rounding margin, and the quotients' own error is below 1e-3 voxel)
     const float ivd = 1.f / g.vd;
-    const int i0 = max(0, (int)floorf((lo.x - 0.5f * g.vd) * ivd) - g.sx - 1);
-    const int i1 = min(g.dx - 1, (int)ceilf((hi.x - 0.5f * g.vd) * ivd) - g.sx + 1);
-    const int j0 = max(0, (int)floorf((lo.y - 0.5f * g.vd) * ivd) - g.sy - 1);
-    const int j1 = min(g.dy - 1, (int)ceilf((hi.y - 0.5f * g.vd) * ivd) - g.sy + 1);
-    const int k0 = max(0, (int)floorf((lo.z - 0.5f * g.vd) * ivd) - g.sz - 1);
-    const int k1 = min(g.dz - 1, (int)ceilf((hi.z - 0.5f * g.vd) * ivd) - g.sz + 1);
+    const int i0 = max(0, (int)floorf((lo.x - 0.5f * g.vd) * ivd) - g.sx);
+    const int i1 = min(g.dx - 1, (int)ceilf((hi.x - 0.5f * g.vd) * ivd) - g.sx);
+    const int j0 = max(0, (int)floorf((lo.y - 0.5f * g.vd) * ivd) - g.sy);
+    const int j1 = min(g.dy - 1, (int)ceilf((hi.y - 0.5f * g.vd) * ivd) - g.sy);
+    const int k0 = max(0, (int)floorf((lo.z - 0.5f * g.vd) * ivd) - g.sz);
+    const int k1 = min(g.dz - 1, (int)ceilf((hi.z - 0.5f * g.vd) * ivd) - g.sz);
     if (i0 > i1 || j0 > j1 || k0 > k1) return;
     // the boxes of the range, from `first` in steps of `step` (the callers' lanes)
     const int x0 = i0 / kIntTx, y0 = j0 / kIntTy, z0 = k0 / zchunk;
