@@ -63,7 +63,7 @@ int depth_bound_tiles(int H, int W);
 float depth_band_eps(const Camera& cam);
 // largest |K^-1 (u, v, 1)| over the image (with a margin)
 float ray_norm_max(const Camera& cam);
-// projective TSDF update (projective_tsdf.cu:5-140) in 32x8x16 voxel boxes, skipping
+// projective TSDF update (projective_tsdf.cu:5-140) in 32x8x8 voxel boxes, skipping
 // the boxes that provably hold no updated voxel: a marking pass over the depth tiles
 // marks (mark[box] = 1) every box a tile's pixels can update, a compaction lists the
 // marked boxes after the marks and clears the marks, and a persistent pass updates the

@@ -195,7 +195,7 @@ __global__ void __launch_bounds__(256) integrate_prep_batch_kernel(const SceneDe
 // corner tests cost more than the voxels it removed: 48.9 -> 44.7 us per c1 frame
 // without it.)
 constexpr int kIntTx = 32, kIntTy = 8;
-constexpr int kZB = 4;  // voxels of a column segment whose loads are issued together
+constexpr int kZB = 4;  // voxels of a column segment whose loads are issued together (batched scenes)
 
 // The frame's constants of integration beside the pose (which the kernels read from
 // State).
@@ -396,7 +396,7 @@ __device__ __forceinline__ bool box_live(int bx, int by, int bz, int lane, const
     return !band_culled(fp, dmin, dmax, p, g, st);
 }
 
-template <class Vol, bool FIRST>
+template <class Vol, bool FIRST, int ZB = kZB>
 __device__ __forceinline__ void integrate_at(const Vol& vol, const float2* __restrict__ tab,
                                              const State* __restrict__ st, const Grid& g, const IntegrateParams& p,
                                              int bx, int by, int bz)
@@ -432,16 +432,17 @@ __device__ __forceinline__ void integrate_at(const Vol& vol, const float2* __res
     const float ulo = 0.5f - 1e-3f, uhi = (float)W + 0.5f + 1e-3f * (float)W;
     const float vlo = 0.5f - 1e-3f, vhi = (float)H + 0.5f + 1e-3f * (float)H;
     const float inv_trunc = 1.f / g.trunc;
-    // The column segment in batches of kZB voxels: a batch first runs every voxel's tests
+    // The column segment in batches of ZB voxels: a batch first runs every voxel's tests
     // up to its pixel, then issues the table loads of the voxels that reach one together,
     // then the volume loads of the voxels that are updated, so that a thread's loads
     // overlap instead of following one another.  Each voxel is read and written by its
-    // own thread only, so the order changes no value.  (41.9 against 45.6 us per c1 frame
-    // with the listed boxes; the pass is a per-box latency chain.)
-    for (int zb = z0; zb < z1; zb += kZB, lin += kZB * zstride) {
-        int pix[kZB];
+    // own thread only, so the order changes no value.  (The listed boxes' pass is a
+    // per-box latency chain: 41.9 against 45.6 us per c1 frame for batches of 4 in 16-voxel
+    // segments, 36.1 against 37.3 us for one batch of 8 in 8-voxel segments.)
+    for (int zb = z0; zb < z1; zb += ZB, lin += ZB * zstride) {
+        int pix[ZB];
 #pragma unroll
-        for (int k = 0; k < kZB; ++k) {
+        for (int k = 0; k < ZB; ++k) {
             const int z = zb + k;
             pix[k] = -1;
             if (z >= z1 || (may_skip && rbase + z >= p.skip_from)) continue;
@@ -463,13 +464,13 @@ __device__ __forceinline__ void integrate_at(const Vol& vol, const float2* __res
             if (u < 1 || u > W || v < 1 || v > H) continue;
             pix[k] = (v - 1) * W + (u - 1);
         }
-        float2 e[kZB];
+        float2 e[ZB];
 #pragma unroll
-        for (int k = 0; k < kZB; ++k) e[k] = pix[k] >= 0 ? __ldg(tab + pix[k]) : make_float2(qnan(), 0.f);
-        float fv[kZB];
-        bool upd[kZB];
+        for (int k = 0; k < ZB; ++k) e[k] = pix[k] >= 0 ? __ldg(tab + pix[k]) : make_float2(qnan(), 0.f);
+        float fv[ZB];
+        bool upd[ZB];
 #pragma unroll
-        for (int k = 0; k < kZB; ++k) {
+        for (int k = 0; k < ZB; ++k) {
             upd[k] = false;
             fv[k] = 0.f;
             if (isnan(e[k].x)) continue;
@@ -489,17 +490,17 @@ __device__ __forceinline__ void integrate_at(const Vol& vol, const float2* __res
         }
         if (FIRST) {
 #pragma unroll
-            for (int k = 0; k < kZB; ++k)
+            for (int k = 0; k < ZB; ++k)
                 if (upd[k]) vol.store(lin + k * zstride, fv[k], 1.0f);
         } else {
-            float t[kZB], w[kZB];
+            float t[ZB], w[ZB];
 #pragma unroll
-            for (int k = 0; k < kZB; ++k) {
+            for (int k = 0; k < ZB; ++k) {
                 t[k] = w[k] = 0.f;
                 if (upd[k]) vol.load(lin + k * zstride, t[k], w[k]);
             }
 #pragma unroll
-            for (int k = 0; k < kZB; ++k) {
+            for (int k = 0; k < ZB; ++k) {
                 if (!upd[k]) continue;
                 const float tk = isnan(t[k]) ? 0.0f : t[k];
                 const float wk = isnan(w[k]) ? 0.0f : w[k];
@@ -692,10 +693,13 @@ __global__ void __launch_bounds__(256) integrate_list_kernel(State* st, unsigned
 }
 
 // Persistent: the blocks take the boxes on the mark list in strides of the grid (the
-// list is in marking order, which spreads neighbouring boxes over the blocks); a block
-// of 32 x 8 threads updates one box at a time, a thread its 16-voxel column segment.
+// list is in box order); a block of 32 x 8 threads updates one 32 x 8 x 8 box at a time,
+// a thread its 8-voxel column segment with the loads of all eight issued together (no
+// spills at four blocks per SM).
+constexpr int kListZB = 8;
+
 template <class Vol, bool FIRST>
-__global__ void __launch_bounds__(kIntTx* kIntTy, 5) integrate_kernel(Vol vol, const float2* __restrict__ tab,
+__global__ void __launch_bounds__(kIntTx* kIntTy, 4) integrate_kernel(Vol vol, const float2* __restrict__ tab,
                                                                    const State* __restrict__ st, Grid g,
                                                                    IntegrateParams p,
                                                                    const unsigned* __restrict__ mark, int nbx, int nby,
@@ -709,7 +713,7 @@ __global__ void __launch_bounds__(kIntTx* kIntTy, 5) integrate_kernel(Vol vol, c
     const unsigned* list = mark + nboxes;
     for (unsigned i = blockIdx.x; i < n; i += gridDim.x) {
         const int box = (int)list[i];
-        integrate_at<Vol, FIRST>(vol, tab, st, g, p, box % nbx, (box / nbx) % nby, box / (nbx * nby));
+        integrate_at<Vol, FIRST, kListZB>(vol, tab, st, g, p, box % nbx, (box / nbx) % nby, box / (nbx * nby));
     }
 }
 
@@ -1217,12 +1221,12 @@ int integrate_blocks()
     static int blocks[64] = {};
     int dev = 0;
     cudaGetDevice(&dev);
-    if (dev < 0 || dev >= 64) return 152 * 5;
+    if (dev < 0 || dev >= 64) return 152 * 4;
     if (!blocks[dev]) {
         int sms = 0, per_sm = 0;
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, integrate_kernel<VolF16, false>, kIntTx * kIntTy, 0);
-        blocks[dev] = (sms > 0 ? sms : 152) * (per_sm > 0 ? per_sm : 5);
+        blocks[dev] = (sms > 0 ? sms : 152) * (per_sm > 0 ? per_sm : 4);
     }
     return blocks[dev];
 }
@@ -1267,7 +1271,7 @@ float ray_norm_max(const Camera& cam)
 }
 
 namespace {
-constexpr int kZChunk = 16;
+constexpr int kZChunk = 8;  // voxels along z per box of the single-scene integration
 
 IntegrateParams host_params(const Camera& cam, int zchunk, long long skip_from)
 {

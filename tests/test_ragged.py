@@ -1,6 +1,6 @@
 """Ragged sizes.  The image is 157 x 117 = 18 369 pixels: 287 ICP groups of 64 and one
 pixel, and sides that are not multiples of the ray cast's 8 x 4 tiles.  The grid is
-173 x 161 x 147 voxels, no side a multiple of integration's 32 x 8 x 16 boxes.  The
+173 x 161 x 147 voxels, no side a multiple of integration's 32 x 8 x 8 boxes.  The
 pyramid case uses 156 x 116 (divisible by 4, as three levels need), whose levels hold
 18 096, 4 524 and 1 131 pixels.
 
