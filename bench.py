@@ -479,7 +479,7 @@ def roofline_of(cfg, r, form: str):
                "raycast": "raycast_kernel"}
     keys = {"integration": f"integration_{tsdf}", "icp": f"icp_{form}", "raycast": f"raycast_{tsdf}"}
     # what limits each stage (ncu evidence in profiles/): none of them is HBM-bound
-    limiter = {"integration": "latency: the update's per-box chain over the boxes marked from the depth tiles' frusta",
+    limiter = {"integration": "instruction issue: every voxel of the boxes marked from the depth tiles' frusta projected and tested",
                "icp": "latency: a serial chain of 10 association / reduction / solve passes, L2-resident",
                "raycast": "instruction issue (ALU pipe), L2-resident gathers"}
     stages = {}
