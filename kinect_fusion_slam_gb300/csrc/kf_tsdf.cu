@@ -552,10 +552,11 @@ constexpr float kSlab = 80.f;     // mm of camera depth per slab
 constexpr int kMarkLanes = 8;     // lanes per depth tile (slabs over them)
 
 constexpr float kNearZ = 100.f;   // slabs start at this camera depth
-constexpr float kNearR = 250.f;   // mm around the camera centre marked unconditionally
+constexpr float kNearR = 250.f;   // mm around the camera centre listed when a band reaches kNearZ
+                                  // (at least kNearZ times the largest ray norm)
 
 __device__ __forceinline__ void mark_world_box(float3 lo, float3 hi, const Grid& g, unsigned* __restrict__ mark,
-                                               int zchunk, int nbx, int nby, int nbz, int first = 0, int step = 1)
+                                               int zchunk, int nbx, int nby)
 {
     // the grid's extent with a voxel to spare (the conversions below stay in range); NaN
     // corners (a NaN pose, which updates nothing) leave lo > hi
@@ -576,18 +577,19 @@ __device__ __forceinline__ void mark_world_box(float3 lo, float3 hi, const Grid&
     const int k0 = max(0, (int)floorf((lo.z - 0.5f * g.vd) * ivd) - g.sz);
     const int k1 = min(g.dz - 1, (int)ceilf((hi.z - 0.5f * g.vd) * ivd) - g.sz);
     if (i0 > i1 || j0 > j1 || k0 > k1) return;
-    // the boxes of the range, from `first` in steps of `step` (the callers' lanes)
+    // the boxes holding the range
     const int x0 = i0 / kIntTx, y0 = j0 / kIntTy, z0 = k0 / zchunk;
     const int nx = i1 / kIntTx - x0 + 1, ny = j1 / kIntTy - y0 + 1, nz = k1 / zchunk - z0 + 1;
-    for (int f = first; f < nx * ny * nz; f += step)
+    for (int f = 0; f < nx * ny * nz; ++f)
         mark[((z0 + f / (nx * ny)) * nby + y0 + (f / nx) % ny) * nbx + x0 + f % nx] = 1u;
 }
 
-// kMarkLanes threads per depth tile, the tile's slabs over them; block 0's first warp
-// also marks the boxes around the camera
+// kMarkLanes threads per depth tile, the tile's slabs over them; a tile whose band
+// reaches below kNearZ sets mark_near, and the compaction then lists the boxes around
+// the camera too
 __global__ void __launch_bounds__(256) integrate_mark_kernel(const float2* __restrict__ tab, State* st, Grid g,
                                                              IntegrateParams p, unsigned* __restrict__ mark, int nbx,
-                                                             int nby, int nbz)
+                                                             int nby)
 {
     wait_for_producer();
     // the compaction may be scheduled now; it waits for this kernel before reading marks
@@ -638,14 +640,31 @@ __global__ void __launch_bounds__(256) integrate_mark_kernel(const float2* __res
         wr[c] = make_float3(T[0] * X + T[1] * Y + T[2], T[4] * X + T[5] * Y + T[6], T[8] * X + T[9] * Y + T[10]);
     }
     const float rmax = fmaxf(fmaxf(fabsf(rx0), fabsf(rx1)), fmaxf(fabsf(ry0), fabsf(ry1)));
-    for (int k = lane; k < nslab; k += kMarkLanes) {
-        const float za = z_lo + (float)k * kSlab, zb = fminf(z_lo + (float)(k + 1) * kSlab, z_b);
-        // the slab's corners t + z R (x/z, y/z, 1) for z = za, zb; each coordinate is
-        // within a relative 2^-20 of its terms' magnitudes, covered by e (and a millimetre)
+    // Voxels behind the camera.  The in-front test is a . (c - t) > 0 with a = R ca,
+    // ca = K^-1 (cy, cx, 1) (the reference's swapped principal point), i.e. ca . l > 0 for
+    // the voxel's camera coordinates l = lz (X, Y, 1): lz s(X, Y) > 0 with s = ca_x X +
+    // ca_y Y + 1.  A voxel behind the camera (lz < 0) projects, mirrored, to the pixel of
+    // (X, Y) as well, and passes where s < 0: with a wide field of view and cx far from
+    // cy the reference updates such voxels (|lz| in the same band).  The test's rounding
+    // (the axis against the translation, the dot product) is below 2^-19 (|ca| + 2 tmax)
+    // |lz| lam_max, so where s exceeds twice that over the tile's widened rays (s is
+    // linear: its minimum is at a corner) no voxel behind the camera is updated through
+    // the tile; elsewhere the slabs are marked mirrored too (z from -z_b to -z_lo).
+    const float ca_x = (p.cy - p.cx) / p.fx, ca_y = (p.cx - p.cy) / p.fy;
+    const float s_min = 1.f + fminf(ca_x * rx0, ca_x * rx1) + fminf(ca_y * ry0, ca_y * ry1);
+    const float s_margin = 0x1p-18f * (1.f + fabsf(ca_x) + fabsf(ca_y) + 2.f * tmax) * p.lam_max + 1e-3f;
+    const int nside = s_min > s_margin ? 1 : 2;
+    for (int k = lane; k < nside * nslab; k += kMarkLanes) {
+        const int ks = k < nslab ? k : k - nslab;
+        const float sgn = k < nslab ? 1.f : -1.f;
+        const float za = z_lo + (float)ks * kSlab, zb = fminf(z_lo + (float)(ks + 1) * kSlab, z_b);
+        // the slab's corners t + z R (x/z, y/z, 1) for z = za, zb (or -za, -zb); each
+        // coordinate is within a relative 2^-20 of its terms' magnitudes, covered by e
+        // (and a millimetre)
         float3 lo = make_float3(INFINITY, INFINITY, INFINITY), hi = make_float3(-INFINITY, -INFINITY, -INFINITY);
 #pragma unroll
         for (int c = 0; c < 8; ++c) {
-            const float z = (c & 4) ? zb : za;
+            const float z = sgn * ((c & 4) ? zb : za);
             const float3 w = wr[c & 3];
             const float wx = w.x * z + T[3], wy = w.y * z + T[7], wz = w.z * z + T[11];
             lo = make_float3(fminf(lo.x, wx), fminf(lo.y, wy), fminf(lo.z, wz));
@@ -654,14 +673,14 @@ __global__ void __launch_bounds__(256) integrate_mark_kernel(const float2* __res
         const float e = 0x1p-17f * ((2.f * rmax + 1.f) * 2.f * zb + tmax) + 1.f;
         lo = make_float3(lo.x - e, lo.y - e, lo.z - e);
         hi = make_float3(hi.x + e, hi.y + e, hi.z + e);
-        mark_world_box(lo, hi, g, mark, p.zchunk, nbx, nby, nbz);
+        mark_world_box(lo, hi, g, mark, p.zchunk, nbx, nby);
     }
 }
 
 // The marked boxes in order, as a list after the marks (mark + nboxes), and the marks
 // cleared: one thread per box, one atomic per warp for the warp's marked boxes.
 __global__ void __launch_bounds__(256) integrate_list_kernel(State* st, unsigned* __restrict__ mark, Grid g,
-                                                             int zchunk, int nbx, int nby, int nboxes)
+                                                             int zchunk, int nbx, int nby, int nboxes, float near_r)
 {
     wait_for_producer();
     // integration may be scheduled now; it waits for this kernel before reading the list
@@ -670,10 +689,10 @@ __global__ void __launch_bounds__(256) integrate_list_kernel(State* st, unsigned
     const int lane = threadIdx.x & 31;
     bool m = b < nboxes && mark[b] != 0u;
     if (!m && b < nboxes && st->mark_near) {
-        // the box's voxel centres against the camera centre widened by kNearR (and two
+        // the box's voxel centres against the camera centre widened by near_r (and two
         // voxels for the rounding of both)
         const int bx = b % nbx, by = (b / nbx) % nby, bz = b / (nbx * nby);
-        const float r = kNearR + 2.f * g.vd;
+        const float r = near_r + 2.f * g.vd;
         const auto overlaps = [&](int i0, int n, int s0, float c) {
             const float lo = ((float)(i0 + s0) + 0.5f) * g.vd, hi = ((float)(i0 + n - 1 + s0) + 0.5f) * g.vd;
             return hi >= c - r && lo <= c + r;
@@ -1288,10 +1307,13 @@ void integrate_launch(Vol vol, const float2* tab, const State* st, const Grid& g
     const dim3 grid((g.dx + kIntTx - 1) / kIntTx, (g.dy + kIntTy - 1) / kIntTy, (g.dz + kZChunk - 1) / kZChunk);
     const int nboxes = (int)(grid.x * grid.y * grid.z);
     launch_pdl(integrate_mark_kernel, dim3((depth_bound_tiles(cam.H, cam.W) * kMarkLanes + 255) / 256), dim3(256), 0, s,
-               tab, const_cast<State*>(st), g, p,
-               mark, (int)grid.x, (int)grid.y, (int)grid.z);
+               tab, const_cast<State*>(st), g, p, mark, (int)grid.x, (int)grid.y);
+    // a voxel updated with camera depth lz < kNearZ lies within kNearZ max|K^-1 (u, v, 1)|
+    // of the camera centre (the ray norm at the image's corner pixels, with a 1 % margin
+    // that covers the half pixel beyond them)
+    const float near_r = std::max(kNearR, kNearZ * p.lam_max);
     launch_pdl(integrate_list_kernel, dim3((nboxes + 255) / 256), dim3(256), 0, s, const_cast<State*>(st), mark, g,
-               p.zchunk, (int)grid.x, (int)grid.y, nboxes);
+               p.zchunk, (int)grid.x, (int)grid.y, nboxes, near_r);
     const dim3 blocks(integrate_blocks());
     if (first)
         launch_pdl(integrate_kernel<Vol, true>, blocks, block, 0, s, vol, tab, st, g, p, (const unsigned*)mark,

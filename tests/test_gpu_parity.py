@@ -136,6 +136,44 @@ def test_integration_cull_exact(oracle, small_seq, offset_vox):
     assert np.count_nonzero(~np.isnan(wo)) > 1000
 
 
+def test_integration_cull_exact_wide_angle(oracle, small_seq):
+    """A wide-angle camera (focal length 30 px on 160 x 120: rays up to 3.5 times their
+    depth long at the corners) with many depths of 50-150 mm: the voxels updated closer
+    than the marking's first slab lie up to ~350 mm from the camera centre, beyond the
+    default near radius, and must still be listed.  Bit for bit against the oracle."""
+    seq, _ = small_seq
+    g = seq.cfg.grid
+    cam = seq.cfg.camera
+    H, W = cam.height, cam.width
+    h = kf.Handle(kf.make_config(height=H, width=W, dims=g.dims, grid_start=g.start, voxel_size=g.voxel_size))
+    K = np.array([[30.0, 0.0, W / 2 + 0.5], [0.0, 30.0, H / 2 + 0.5], [0.0, 0.0, 1.0]], np.float32)
+    h.set_intrinsics(K[0, 0], K[1, 1], K[0, 2], K[1, 2])
+    gs = grid_spec(g)
+    Ki = oracle.inv3(K)
+    rng = np.random.default_rng(17)
+    to = np.full(gs.nvox, np.nan, np.float32)
+    wo = np.full(gs.nvox, np.nan, np.float32)
+    poses = [(0.3, 0.2, 0.0, (200.0, -150.0, -300.0)), (-0.5, -0.25, 0.3, (-400.0, 300.0, 100.0)),
+             (1.2, 0.1, -0.2, (0.0, 0.0, 500.0))]
+    for n, (yaw, pitch, roll, t) in enumerate(poses):
+        T = np.eye(4)
+        T[:3, :3] = _rot(yaw, pitch, roll)
+        T[:3, 3] = t
+        T = T.astype(np.float32)
+        yy, xx = np.mgrid[0:H, 0:W]
+        depth = (400.0 + 300.0 * np.sin(xx / 9.0) * np.cos(yy / 7.0)).astype(np.float32)
+        near = rng.random((H, W)) < 0.1
+        depth[near] = rng.uniform(50.0, 150.0, int(near.sum())).astype(np.float32)
+        depth[rng.random((H, W)) < 0.1] = 0.0
+        h.set_pose(T)
+        h.set_depth_f32(depth)
+        h.projective_tsdf(first=(n == 0))
+        oracle.integrate(gs, depth, K, Ki, T, oracle.inv4(T), to, wo, first=(n == 0))
+        tg, wg = h.volume()
+        assert_volume_parity(tg, wg, to, wo)
+    assert np.count_nonzero(~np.isnan(wo)) > 1000
+
+
 def test_raycast(oracle, small_seq):
     seq, depths = small_seq
     gs = grid_spec(seq.cfg.grid)
