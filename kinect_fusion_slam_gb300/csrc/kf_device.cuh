@@ -54,6 +54,7 @@ struct State {
     float c_flip;         // ray-cast normal flip threshold (voxel_traversal.cu:361-369)
     unsigned mark_count;  // boxes on integration's mark list (reset by integrate_prep)
     unsigned mark_near;   // some tile's depth band reaches near the camera (reset likewise)
+    unsigned mark_all;    // some tile's band has no finite depth bound: every box is listed (likewise)
     double Td[16];        // FP64 pose (precise solve mode)
     unsigned ticket;      // last-block election counter of the ICP reduction
     int iter;             // ICP iterations done in the current frame

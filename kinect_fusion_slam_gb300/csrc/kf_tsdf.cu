@@ -141,6 +141,7 @@ __device__ __forceinline__ void integrate_prep_tile(int tile, int lane, const fl
         if (lane == 0) {
             st->mark_count = 0u;
             st->mark_near = 0u;
+            st->mark_all = 0u;
         }
     }
     float lo = INFINITY, hi = -INFINITY;
@@ -549,6 +550,7 @@ __device__ __forceinline__ void integrate_box(const Vol& vol, const float2* __re
 // the boxes within kNearR of the camera centre are listed too (the compaction tests
 // each box against the camera).
 constexpr float kSlab = 80.f;     // mm of camera depth per slab
+constexpr int kMaxSlabs = 512;    // per tile and side (thicker slabs beyond)
 constexpr int kMarkLanes = 8;     // lanes per depth tile (slabs over them)
 
 constexpr float kNearZ = 100.f;   // slabs start at this camera depth
@@ -612,11 +614,36 @@ __global__ void __launch_bounds__(256) integrate_mark_kernel(const float2* __res
     const float abs_t = 0x1p-19f * tmax + 1.f;
     const float hi_band = fmaxf(g.sdf_max, 0.f), lo_band = fminf(g.sdf_min, 0.f);
     const float z_a = (dmin * (1.f - eps_t) - hi_band - 2.f * abs_t) / ((1.f + p.depth_eps) * (1.f + eps_t)) * 0.999f - 1.f;
-    const float z_b = (dmax * (1.f + eps_t) - lo_band + 2.f * abs_t) / ((1.f - p.depth_eps) * (1.f - eps_t)) * 1.001f + 1.f;
+    // (for a camera some hundreds of metres from the origin eps_t nears 1 and z_b has no
+    // bound of its own; the grid's far side below bounds the slabs then)
+    const float den_b = (1.f - p.depth_eps) * (1.f - eps_t);
+    const float z_b = den_b > 0.5f ? (dmax * (1.f + eps_t) - lo_band + 2.f * abs_t) / den_b * 1.001f + 1.f : INFINITY;
     if (z_a < kNearZ && lane == 0) st->mark_near = 1u;  // the boxes around the camera too
-    const float z_lo = fmaxf(z_a, kNearZ);
-    if (!(z_b > z_lo)) return;
-    const int nslab = (int)ceilf((z_b - z_lo) / kSlab);
+    // A voxel's |lz| is at most its distance from the camera centre (with 1 % for a pose
+    // a little off orthonormal and for the rounding of lz), and no voxel centre lies
+    // farther than the grid's farthest corner centre: the slabs end there, so a depth of
+    // 1e30 or inf costs no more slabs than the grid's own depth.  A NaN pose updates
+    // nothing.
+    float far2 = 0.f;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const int s0 = a == 0 ? g.sx : a == 1 ? g.sy : g.sz, n = a == 0 ? g.dx : a == 1 ? g.dy : g.dz;
+        const float t = T[4 * a + 3];
+        const float d = fmaxf(fabsf(((float)s0 + 0.5f) * g.vd - t), fabsf(((float)(s0 + n) - 0.5f) * g.vd - t));
+        far2 += d * d;
+    }
+    const float z_far = sqrtf(far2) * 1.01f + 2.f * g.vd + 1.f;
+    if (isnan(z_far)) return;
+    const float z_lo = fmaxf(z_a, kNearZ), z_hi = fminf(z_b, z_far);
+    if (!(z_hi > z_lo)) return;
+    const float span = z_hi - z_lo;
+    if (!(span < 1e30f)) {  // no finite bound (an infinite translation): every box
+        if (lane == 0) st->mark_all = 1u;
+        return;
+    }
+    // slabs of kSlab, thicker where the span would need more than kMaxSlabs of them
+    const float slab = fmaxf(kSlab, span * (1.f / (float)kMaxSlabs));
+    const int nslab = min(kMaxSlabs, (int)ceilf(span / slab));
     // rounding error of a voxel's camera coordinates (integrate_at's evaluation): at
     // most 2^-19 of a generous bound on their terms' magnitudes, the grid's extent plus
     // the camera's distance from the origin; the pixel margin is taken at the nearest
@@ -649,7 +676,7 @@ __global__ void __launch_bounds__(256) integrate_mark_kernel(const float2* __res
     // (the axis against the translation, the dot product) is below 2^-19 (|ca| + 2 tmax)
     // |lz| lam_max, so where s exceeds twice that over the tile's widened rays (s is
     // linear: its minimum is at a corner) no voxel behind the camera is updated through
-    // the tile; elsewhere the slabs are marked mirrored too (z from -z_b to -z_lo).
+    // the tile; elsewhere the slabs are marked mirrored too (z from -z_hi to -z_lo).
     const float ca_x = (p.cy - p.cx) / p.fx, ca_y = (p.cx - p.cy) / p.fy;
     const float s_min = 1.f + fminf(ca_x * rx0, ca_x * rx1) + fminf(ca_y * ry0, ca_y * ry1);
     const float s_margin = 0x1p-18f * (1.f + fabsf(ca_x) + fabsf(ca_y) + 2.f * tmax) * p.lam_max + 1e-3f;
@@ -657,7 +684,8 @@ __global__ void __launch_bounds__(256) integrate_mark_kernel(const float2* __res
     for (int k = lane; k < nside * nslab; k += kMarkLanes) {
         const int ks = k < nslab ? k : k - nslab;
         const float sgn = k < nslab ? 1.f : -1.f;
-        const float za = z_lo + (float)ks * kSlab, zb = fminf(z_lo + (float)(ks + 1) * kSlab, z_b);
+        const float za = z_lo + (float)ks * slab;
+        const float zb = ks == nslab - 1 ? z_hi : fminf(z_lo + (float)(ks + 1) * slab, z_hi);
         // the slab's corners t + z R (x/z, y/z, 1) for z = za, zb (or -za, -zb); each
         // coordinate is within a relative 2^-20 of its terms' magnitudes, covered by e
         // (and a millimetre)
@@ -687,7 +715,7 @@ __global__ void __launch_bounds__(256) integrate_list_kernel(State* st, unsigned
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     const int b = blockIdx.x * blockDim.x + threadIdx.x;
     const int lane = threadIdx.x & 31;
-    bool m = b < nboxes && mark[b] != 0u;
+    bool m = b < nboxes && (mark[b] != 0u || st->mark_all != 0u);
     if (!m && b < nboxes && st->mark_near) {
         // the box's voxel centres against the camera centre widened by near_r (and two
         // voxels for the rounding of both)

@@ -88,14 +88,15 @@ def _rot(yaw, pitch, roll):
     return Ry @ Rx @ Rz
 
 
-@pytest.mark.parametrize("offset_vox", [0, 2500])
+@pytest.mark.parametrize("offset_vox", [0, 2500, 16000])
 def test_integration_cull_exact(oracle, small_seq, offset_vox):
     """Integration skips voxel boxes and column segments that provably hold no updated
     voxel (behind the camera, outside the image, or beyond the truncation band of every
     depth their pixels can read).  Hard cases for those proofs, bit for bit against the
     oracle: oblique camera poses inside the grid, depths from 0.1 to 6 m with holes,
-    negative and isolated near samples, and the whole scene moved 50 m from the origin
-    (larger rounding against the translation)."""
+    negative and isolated near samples, and the whole scene moved 50 m or 320 m from the
+    origin (larger rounding against the translation; at 320 m the marks' depth band has
+    no far bound of its own and the grid's far side bounds it)."""
     seq, _ = small_seq
     g = seq.cfg.grid
     cam = seq.cfg.camera
@@ -165,6 +166,32 @@ def test_integration_cull_exact_wide_angle(oracle, small_seq):
         near = rng.random((H, W)) < 0.1
         depth[near] = rng.uniform(50.0, 150.0, int(near.sum())).astype(np.float32)
         depth[rng.random((H, W)) < 0.1] = 0.0
+        h.set_pose(T)
+        h.set_depth_f32(depth)
+        h.projective_tsdf(first=(n == 0))
+        oracle.integrate(gs, depth, K, Ki, T, oracle.inv4(T), to, wo, first=(n == 0))
+        tg, wg = h.volume()
+        assert_volume_parity(tg, wg, to, wo)
+    assert np.count_nonzero(~np.isnan(wo)) > 1000
+
+
+def test_integration_huge_depths(oracle, small_seq):
+    """Depths of 1e7 mm, 1e30 mm and +inf beside the sequence's own (float input, no
+    range filter): the marks' slabs end at the grid's far side, so the marking pass stays
+    as short as for ordinary depths, and the volume is bit for bit the oracle's."""
+    seq, depths = small_seq
+    gs = grid_spec(seq.cfg.grid)
+    h = make_handle(seq)
+    K = seq.K
+    Ki = oracle.inv3(K)
+    rng = np.random.default_rng(23)
+    to = np.full(gs.nvox, np.nan, np.float32)
+    wo = np.full(gs.nvox, np.nan, np.float32)
+    for n, k in enumerate([0, 1, 2]):
+        T = seq.poses[k].astype(np.float32)
+        depth = oracle.depth_ingest(depths[k]).copy()
+        for value, frac in [(1e7, 0.02), (1e30, 0.02), (np.inf, 0.02)]:
+            depth[rng.random(depth.shape) < frac] = value
         h.set_pose(T)
         h.set_depth_f32(depth)
         h.projective_tsdf(first=(n == 0))
