@@ -11,6 +11,7 @@
 // 32 consecutive voxels.
 #include "kf_kernels.h"
 #include "kf_launch.cuh"
+#include "kf_rigid.h"
 
 namespace kf {
 
@@ -603,6 +604,9 @@ __global__ void __launch_bounds__(256) integrate_mark_kernel(const float2* __res
 #pragma unroll
     for (int k = 0; k < 12; ++k) T[k] = st->T[k];
     const float tmax = fmaxf(fmaxf(fabsf(T[3]), fabsf(T[7])), fabsf(T[11]));
+    // the margins below hold for a rotation within kRigidTol of orthonormal; a pose
+    // further off has every box listed
+    if (blockIdx.x == 0 && threadIdx.x == 0 && rigid_error(T) > kRigidTol) st->mark_all = 1u;
     if (tile >= tiles) return;
     const float2 b = tab[p.H * p.W + tile];
     const float dmin = b.x, dmax = b.y;
@@ -674,12 +678,15 @@ __global__ void __launch_bounds__(256) integrate_mark_kernel(const float2* __res
     // (X, Y) as well, and passes where s < 0: with a wide field of view and cx far from
     // cy the reference updates such voxels (|lz| in the same band).  The test's rounding
     // (the axis against the translation, the dot product) is below 2^-19 (|ca| + 2 tmax)
-    // |lz| lam_max, so where s exceeds twice that over the tile's widened rays (s is
-    // linear: its minimum is at a corner) no voxel behind the camera is updated through
-    // the tile; elsewhere the slabs are marked mirrored too (z from -z_hi to -z_lo).
+    // |lz| lam_max, and a rotation off orthonormal by up to kRigidTol moves the test by
+    // 2 kRigidTol |ca| |lz| lam_max at most; where s exceeds twice their sum over the
+    // tile's widened rays (s is linear: its minimum is at a corner) no voxel behind the
+    // camera is updated through the tile; elsewhere the slabs are marked mirrored too (z
+    // from -z_hi to -z_lo).
     const float ca_x = (p.cy - p.cx) / p.fx, ca_y = (p.cx - p.cy) / p.fy;
     const float s_min = 1.f + fminf(ca_x * rx0, ca_x * rx1) + fminf(ca_y * ry0, ca_y * ry1);
-    const float s_margin = 0x1p-18f * (1.f + fabsf(ca_x) + fabsf(ca_y) + 2.f * tmax) * p.lam_max + 1e-3f;
+    const float ca_n = 1.f + fabsf(ca_x) + fabsf(ca_y);
+    const float s_margin = (0x1p-18f * (ca_n + 2.f * tmax) + 4.f * kRigidTol * ca_n) * p.lam_max + 1e-3f;
     const int nside = s_min > s_margin ? 1 : 2;
     for (int k = lane; k < nside * nslab; k += kMarkLanes) {
         const int ks = k < nslab ? k : k - nslab;
