@@ -101,7 +101,10 @@ kf_status kf_set_intrinsics(kf_handle* h, float fx, float fy, float cx, float cy
  * one_based == 0 takes a 0-based (cx, cy), stored as (cx + 1, cy + 1) in float */
 kf_status kf_set_intrinsics_ex(kf_handle* h, float fx, float fy, float cx, float cy, int one_based);
 kf_status kf_get_intrinsics(const kf_handle* h, float K[9]);
-/* extrinsic_matrix (kinfu_pipeline.h:18): 4x4 row-major camera-to-world, mm */
+/* extrinsic_matrix (kinfu_pipeline.h:18): 4x4 row-major camera-to-world, mm.  Any
+ * matrix is integrated as the reference does; one whose rotation block is more than 2e-4
+ * from orthonormal (scaled or sheared) makes integration visit every voxel box (exact,
+ * at a dense pass's cost) instead of the boxes its depth tiles can reach. */
 kf_status kf_set_pose(kf_handle* h, const float T[16]);
 /* Right after a frame call, waits only until that frame's pose is final (the end of its
  * ICP; integration and the ray cast go on in the stream); otherwise waits for all work
