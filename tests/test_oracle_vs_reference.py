@@ -154,3 +154,40 @@ def test_reference_integration_skips_last_voxel(oracle, reference):
     reference.integrate(gs, depth, K, Ki, T, oracle.inv4(T), tr, wr, first=True)
     assert np.array_equal(bits(to), bits(tr)) and np.array_equal(bits(wo), bits(wr))
     assert np.isnan(wo[-1])
+
+
+def test_integration_wide_angle_behind_camera(oracle, reference, small_seq):
+    """With a 30 px focal length on 160 x 120 the reference's in-front axis, built from the
+    swapped principal point (projective_tsdf.cu:57-73), tilts far enough that voxels
+    behind the camera pass it and, projecting mirrored into the image, are updated (the
+    GPU's box marks cover them).  The oracle reproduces the reference bit for bit here,
+    with near, infinite, 1e30 and NaN depths among ordinary ones."""
+    seq, _ = small_seq
+    gs = grid_spec(seq.cfg.grid)
+    H, W = seq.cfg.camera.height, seq.cfg.camera.width
+    K = np.array([[30.0, 0.0, W / 2 + 0.5], [0.0, 30.0, H / 2 + 0.5], [0.0, 0.0, 1.0]], np.float32)
+    Ki = oracle.inv3(K)
+    rng = np.random.default_rng(17)
+    c, s = np.cos(0.3), np.sin(0.3)
+    T = np.array([[c, 0, s, 200.0], [0, 1, 0, -150.0], [-s, 0, c, -300.0], [0, 0, 0, 1]], np.float32)
+    yy, xx = np.mgrid[0:H, 0:W]
+    depth = (400.0 + 300.0 * np.sin(xx / 9.0) * np.cos(yy / 7.0)).astype(np.float32)
+    near = rng.random((H, W)) < 0.1
+    depth[near] = rng.uniform(50.0, 150.0, int(near.sum())).astype(np.float32)
+    for value, frac in [(0.0, 0.1), (np.inf, 0.01), (1e30, 0.01), (np.nan, 0.01)]:
+        depth[rng.random((H, W)) < frac] = value
+    vols = {}
+    for name, impl in (("o", oracle), ("r", reference)):
+        t = np.full(gs.nvox, np.nan, np.float32)
+        w = np.full(gs.nvox, np.nan, np.float32)
+        impl.integrate(gs, depth, K, Ki, T, oracle.inv4(T), t, w, first=True)
+        vols[name] = (t, w)
+    assert np.array_equal(bits(vols["o"][0]), bits(vols["r"][0]))
+    assert np.array_equal(bits(vols["o"][1]), bits(vols["r"][1]))
+    # updated voxels behind the camera (z-fastest index: ((x * dy) + y) * dz + z)
+    dims = gs.dims
+    upd = np.flatnonzero(~np.isnan(vols["r"][1]))
+    ijk = np.stack([upd // (dims[1] * dims[2]), (upd // dims[2]) % dims[1], upd % dims[2]], 1)
+    centres = (ijk + np.asarray(gs.start) + 0.5) * gs.voxel_size
+    lz = (centres - T[:3, 3].astype(np.float64)) @ T[:3, 2].astype(np.float64)
+    assert np.count_nonzero(lz < 0) > 1000
