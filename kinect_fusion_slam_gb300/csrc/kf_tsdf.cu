@@ -342,9 +342,13 @@ __device__ __forceinline__ bool band_culled(const Footprint& fp, float dmin, flo
     const float eps_t = 0x1p-18f * (tmax + 4.f * p.lam_max + 1.f);
     const float abs_t = 0x1p-19f * tmax + 1.f;
     const float hi_band = fmaxf(g.sdf_max, 0.f), lo_band = fminf(g.sdf_min, 0.f);
-    const bool all_ahead = fp.lz_hi * (1.f + p.depth_eps) * (1.f + eps_t) + abs_t < dmin * (1.f - eps_t) - hi_band - abs_t;
-    const bool all_behind =
-        fp.lz_lo * (1.f - p.depth_eps) * (1.f - eps_t) - abs_t > dmax * (1.f + eps_t) - lo_band + abs_t;
+    // a rotation block up to kRigidTol off orthonormal scales tm / m against lz by at most
+    // 1 +- 2 kRigidTol (box_live keeps every box for a pose further off)
+    const float rig = 4.f * kRigidTol;
+    const bool all_ahead = fp.lz_hi * (1.f + p.depth_eps) * (1.f + eps_t) * (1.f + rig) + abs_t <
+                           dmin * (1.f - eps_t) - hi_band - abs_t;
+    const bool all_behind = fp.lz_lo * (1.f - p.depth_eps) * (1.f - eps_t) * (1.f - rig) - abs_t >
+                            dmax * (1.f + eps_t) - lo_band + abs_t;
     return all_ahead || all_behind;
 }
 
@@ -369,6 +373,14 @@ __device__ __forceinline__ bool box_live(int bx, int by, int bz, int lane, const
                                          const State* __restrict__ st, const float2* __restrict__ bounds,
                                          const IntegrateParams& p)
 {
+    // the cull's margins hold for a rotation within kRigidTol of orthonormal; a pose
+    // further off keeps every box (the same decision in every lane)
+    {
+        float T[12];
+#pragma unroll
+        for (int k = 0; k < 12; ++k) T[k] = st->T[k];
+        if (rigid_error(T) > kRigidTol) return true;
+    }
     float ti[12], tx, ty, tz, ax, ay, az;
     load_pose(st, ti, tx, ty, tz, ax, ay, az);
     const int c = lane & 7;
@@ -613,7 +625,8 @@ __global__ void __launch_bounds__(256) integrate_mark_kernel(const float2* __res
     if (!(dmin <= dmax)) return;  // no pixel with depth in this tile
     // band_culled's margins: a voxel updated through a pixel with depth D in [dmin, dmax]
     // has z_a <= lz <= z_b (its two tests rearranged for lz); widened by 0.1 % and 1 mm for
-    // the float evaluation of these bounds (a few units in the last place)
+    // the float evaluation of these bounds (a few units in the last place) and a rotation
+    // up to kRigidTol off orthonormal (a factor within 1 +- 2 kRigidTol)
     const float eps_t = 0x1p-18f * (tmax + 4.f * p.lam_max + 1.f);
     const float abs_t = 0x1p-19f * tmax + 1.f;
     const float hi_band = fmaxf(g.sdf_max, 0.f), lo_band = fminf(g.sdf_min, 0.f);
